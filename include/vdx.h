@@ -1,0 +1,157 @@
+/*
+ * vdx.h -- C ABI of libvdx, the GB300 (sm_103a) FFT / FFT-convolution /
+ * reduction library of vkdispatch_gb300.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: VDX_OK (0) or a VDX_ERR_* code.
+ *     On failure nothing is launched and vdx_last_error() returns a message
+ *     (thread-local), mirroring the reference's polled last-error string
+ *     (vkdispatch/base/errors.py:15-28, vkdispatch/backends/cuda_backend/
+ *     helpers.py:42-47).
+ *   - All buffers are caller-owned device pointers (torch tensors, CUDA
+ *     arrays behind __cuda_array_interface__, cudaMalloc'd memory).  Plans
+ *     own only their constant twiddle tables.
+ *   - Execution is enqueue-only on the given CUDA stream (a cudaStream_t
+ *     passed as void*; NULL = legacy default stream), like the reference's
+ *     cuLaunchKernel path (vkdispatch/backends/cuda_backend/
+ *     cuda_primitives.py:163-284).  Plans are immutable after creation and
+ *     may be shared between host threads.
+ *   - Layouts are C order.  complex64 = interleaved (re, im) float32.
+ */
+#ifndef VDX_H
+#define VDX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define VDX_OK 0
+#define VDX_ERR_INVALID 1     /* bad argument, shape or plan */
+#define VDX_ERR_UNSUPPORTED 2 /* valid request outside what the kernels implement */
+#define VDX_ERR_CUDA 3        /* CUDA runtime error (message has the CUDA error string) */
+#define VDX_ERR_NOMEM 4       /* device allocation failed (plan tables only) */
+
+/* element types (storage) */
+#define VDX_C64 0    /* complex64: 2 x float32 */
+#define VDX_C32 1    /* complex32: 2 x float16 (IEEE half) */
+#define VDX_C128 2   /* complex128: 2 x float64 */
+#define VDX_BF16X2 3 /* complex as 2 x bfloat16 */
+#define VDX_F32 4
+#define VDX_F64 5
+#define VDX_I32 6
+#define VDX_U32 7
+
+/* transform kinds */
+#define VDX_KIND_C2C 0  /* complex FFT along one axis, in or out of place */
+#define VDX_KIND_R2C 1  /* real FFT of the last axis, packed RFFT layout */
+#define VDX_KIND_C2R 2  /* inverse real FFT of the last axis, packed RFFT layout */
+#define VDX_KIND_CONV 3 /* fused FFT -> spectrum * op(kernel) -> inverse FFT along one axis */
+
+/* convolution spectrum operations */
+#define VDX_KOP_MUL_CONJ 0 /* spectrum * conj(kernel) (the reference default) */
+#define VDX_KOP_MUL 1      /* spectrum * kernel */
+
+typedef struct vdx_fft_desc {
+  int32_t ndim;       /* 1..4 */
+  int64_t shape[4];   /* buffer shape; for R2C/C2R the REAL shape (last dim N) */
+  int32_t axis;       /* transformed axis (R2C/C2R: must be ndim-1) */
+  int32_t kind;       /* VDX_KIND_* */
+  int32_t inverse;    /* C2C: 0 forward (exp(-2 pi i nk/N)), 1 inverse */
+  int32_t normalize;  /* inverse / C2R / CONV: scale by 1/N */
+  int32_t io_type;    /* VDX_C64, VDX_C32, VDX_C128 or VDX_BF16X2 */
+  int32_t compute_type; /* VDX_C64 (fp32 butterflies) or VDX_C128 (fp64) */
+  int64_t signal_lo;  /* input_signal_range: points outside [lo, hi) read as 0; */
+  int64_t signal_hi;  /* lo = 0, hi = N (or hi <= 0) means the whole axis       */
+  int32_t kernel_op;  /* CONV: VDX_KOP_* */
+  int32_t kernel_type;/* CONV: storage type of the kernel spectrum */
+  int32_t kernel_broadcast; /* CONV: 1 = one kernel spectrum for every outer batch */
+  int32_t reserved;
+} vdx_fft_desc;
+
+typedef struct vdx_plan vdx_plan;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int vdx_version(void);
+
+/* Copies the calling thread's last error message into buf (NUL-terminated). */
+int vdx_last_error(char* buf, size_t n);
+
+/* Number of visible CUDA devices; fails when the driver is unusable. */
+int vdx_device_count(int* count);
+
+/*
+ * Plan creation.  Replaces the reference's kernel factory + runtime compile:
+ * make_fft_shader / make_convolution_shader (vkdispatch/fft/
+ * shader_factories.py:11-60, 107-195) -> FFTConfig plan builder
+ * (vkdispatch/fft/config.py:192-277) -> NVRTC compile and module load
+ * (vkdispatch/backends/cuda_backend/api_compute.py:30-70).  Builds the radix
+ * pass list, launch shape and FP64-built twiddle tables on the current
+ * device.
+ */
+int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan);
+int vdx_fft_plan_destroy(vdx_plan* plan);
+
+/* Human-readable plan (radices, threads per transform, transforms per CTA). */
+int vdx_fft_plan_describe(const vdx_plan* plan, char* buf, size_t n);
+
+/*
+ * Executes a plan: one kernel launch on `stream`.  Replaces the reference's
+ * ShaderFunction.__call__ -> CommandGraph.record_shader -> cuLaunchKernel
+ * path (vkdispatch/shader/shader_function.py:277-380,
+ * vkdispatch/execution_pipeline/command_graph.py:193-279,
+ * vkdispatch/backends/cuda_backend/cuda_primitives.py:163-284).
+ *   in/out : same shape and io_type; in == out is the reference's in-place
+ *            mode.  R2C/C2R use the packed RFFT layout: rows of N/2+1
+ *            complex elements whose first N reals hold the real signal
+ *            (vkdispatch/base/buffer.py:377-448).
+ *   kernel : CONV only; spectrum of the buffer's shape (or one batch of it
+ *            when kernel_broadcast = 1).
+ */
+int vdx_fft_exec(const vdx_plan* plan, const void* in, void* out, const void* kernel, void* stream);
+
+/* reduction operations (vkdispatch/reduce/operations.py:17-66) */
+#define VDX_RED_ADD 0
+#define VDX_RED_MUL 1
+#define VDX_RED_MIN 2
+#define VDX_RED_MAX 3
+#define VDX_RED_AND 4
+#define VDX_RED_OR 5
+#define VDX_RED_XOR 6
+
+/* element-wise maps applied before reducing (the map-hook menu) */
+#define VDX_MAP_IDENTITY 0 /* x                      */
+#define VDX_MAP_ABS 1      /* |x|  (complex: modulus) */
+#define VDX_MAP_SQUARE 2   /* x^2  (complex: |x|^2)   */
+#define VDX_MAP_REAL 3     /* complex: real part      */
+#define VDX_MAP_IMAG 4     /* complex: imaginary part */
+#define VDX_MAP_SIN 5      /* sin(x)                  */
+
+/*
+ * Number of stage-1 partial slots vdx_reduce needs per batch row for a row
+ * of `n` elements; the workspace must hold partial_count * batch elements of
+ * the output type.
+ */
+int vdx_reduce_partial_count(int64_t n, int64_t* partial_count);
+
+/*
+ * Batched map-reduce over rows: out[b] = op over i < n of map(in[b*n + i]).
+ * Replaces ReduceFunction.__call__ and its two generated stages
+ * (vkdispatch/reduce/reduce_function.py:73-162, vkdispatch/reduce/
+ * stage.py:147-186).  Two launches: per-CTA partials into `workspace`, then
+ * one fixed-order pass per row, so results are deterministic for a given n.
+ * in_type: VDX_F32, VDX_F64, VDX_I32, VDX_U32 or VDX_C64 (complex input needs
+ * a map to a real value).  Output type: F32 for F32/C64 input, otherwise the
+ * input type.  Bitwise ops require integer types.
+ */
+int vdx_reduce(int op, int map, int in_type, const void* in, int64_t n, int64_t batch, void* out,
+               void* workspace, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VDX_H */

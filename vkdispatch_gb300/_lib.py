@@ -1,0 +1,126 @@
+"""ctypes binding of libvdx.so (declared in include/vdx.h).
+
+The library is required: there is no CPU or PyTorch fallback.  Loading fails
+with an explicit error when the in-tree build is missing.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libvdx.so"
+
+VDX_OK = 0
+VDX_ERR_INVALID = 1
+VDX_ERR_UNSUPPORTED = 2
+VDX_ERR_CUDA = 3
+VDX_ERR_NOMEM = 4
+
+# element types
+VDX_C64, VDX_C32, VDX_C128, VDX_BF16X2, VDX_F32, VDX_F64, VDX_I32, VDX_U32 = range(8)
+
+# transform kinds
+VDX_KIND_C2C, VDX_KIND_R2C, VDX_KIND_C2R, VDX_KIND_CONV = range(4)
+VDX_KOP_MUL_CONJ, VDX_KOP_MUL = range(2)
+
+# reductions and maps
+VDX_RED_ADD, VDX_RED_MUL, VDX_RED_MIN, VDX_RED_MAX, VDX_RED_AND, VDX_RED_OR, VDX_RED_XOR = range(7)
+VDX_MAP_IDENTITY, VDX_MAP_ABS, VDX_MAP_SQUARE, VDX_MAP_REAL, VDX_MAP_IMAG, VDX_MAP_SIN = range(6)
+
+EXPORTED = (
+    "vdx_version",
+    "vdx_last_error",
+    "vdx_device_count",
+    "vdx_fft_plan_create",
+    "vdx_fft_plan_destroy",
+    "vdx_fft_plan_describe",
+    "vdx_fft_exec",
+    "vdx_reduce_partial_count",
+    "vdx_reduce",
+)
+
+
+class FftDesc(ctypes.Structure):
+    _fields_ = [
+        ("ndim", ctypes.c_int32),
+        ("shape", ctypes.c_int64 * 4),
+        ("axis", ctypes.c_int32),
+        ("kind", ctypes.c_int32),
+        ("inverse", ctypes.c_int32),
+        ("normalize", ctypes.c_int32),
+        ("io_type", ctypes.c_int32),
+        ("compute_type", ctypes.c_int32),
+        ("signal_lo", ctypes.c_int64),
+        ("signal_hi", ctypes.c_int64),
+        ("kernel_op", ctypes.c_int32),
+        ("kernel_type", ctypes.c_int32),
+        ("kernel_broadcast", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+class VdxError(RuntimeError):
+    """Raised for CUDA-side failures reported by libvdx."""
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def _declare(lib: ctypes.CDLL) -> None:
+    vp, i32, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
+    lib.vdx_version.restype = i32
+    lib.vdx_version.argtypes = []
+    lib.vdx_last_error.restype = i32
+    lib.vdx_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    lib.vdx_device_count.restype = i32
+    lib.vdx_device_count.argtypes = [ctypes.POINTER(ctypes.c_int)]
+    lib.vdx_fft_plan_create.restype = i32
+    lib.vdx_fft_plan_create.argtypes = [ctypes.POINTER(FftDesc), ctypes.POINTER(vp)]
+    lib.vdx_fft_plan_destroy.restype = i32
+    lib.vdx_fft_plan_destroy.argtypes = [vp]
+    lib.vdx_fft_plan_describe.restype = i32
+    lib.vdx_fft_plan_describe.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+    lib.vdx_fft_exec.restype = i32
+    lib.vdx_fft_exec.argtypes = [vp, vp, vp, vp, vp]
+    lib.vdx_reduce_partial_count.restype = i32
+    lib.vdx_reduce_partial_count.argtypes = [i64, ctypes.POINTER(i64)]
+    lib.vdx_reduce.restype = i32
+    lib.vdx_reduce.argtypes = [i32, i32, i32, vp, i64, i64, vp, vp, vp]
+
+
+def lib() -> ctypes.CDLL:
+    """Loads libvdx.so once; raises when the in-tree build is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise RuntimeError(
+                    f"libvdx.so not found at {LIB_PATH}; build it with "
+                    "`python -c 'import __graft_entry__ as g; g.build()'` or "
+                    "`python -m vkdispatch_gb300._build` (requires nvcc)"
+                )
+            handle = ctypes.CDLL(str(LIB_PATH))
+            _declare(handle)
+            _lib = handle
+    return _lib
+
+
+def last_error() -> str:
+    buf = ctypes.create_string_buffer(4096)
+    lib().vdx_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int, what: str = "libvdx") -> None:
+    """Maps a libvdx status to the reference's exception types."""
+    if rc == VDX_OK:
+        return
+    msg = f"{what}: {last_error()}"
+    if rc in (VDX_ERR_INVALID, VDX_ERR_UNSUPPORTED):
+        raise ValueError(msg)
+    raise VdxError(msg)

@@ -1,0 +1,469 @@
+// Batched 1-D FFT kernels along one axis of a C-order array, viewed as
+// (outer, N, inner): contiguous axes (inner == 1) and strided axes
+// (inner > 1, "columns").
+//
+// Algorithm: Stockham autosort with a runtime list of radix passes.  Pass p
+// with radix R and Ns = product of the radices before it maps butterfly j to
+//   inputs  j + r*(n/R)                     (r = 0..R-1)
+//   twiddle W_{Ns*R}^{(j mod Ns) * r}
+//   outputs (j - j mod Ns)*R + (j mod Ns) + r*Ns
+// The inputs of the first pass and the outputs of the last pass both sit at
+// j + r*(n/R), so the first pass loads straight from HBM into registers and
+// the last pass stores straight to HBM, both coalesced across threads; only
+// the exchanges between passes go through shared memory.  A fused
+// convolution runs the inverse with the pass order reversed, so the spectrum
+// never leaves registers between the forward and the inverse transform.
+//
+// The reference decomposes the same transforms into per-stage prime groups
+// executed by generated code (vkdispatch/fft/context.py:152-179,
+// vkdispatch/fft/stages.py:104-172); this file is an independent design.
+#pragma once
+
+#include "vdx_common.cuh"
+
+namespace vdx {
+
+constexpr int kMaxPasses = 12;
+
+struct PassPlan {
+  int n;      // complex points per transform
+  int npass;  // number of radix passes
+  int radix[kMaxPasses];
+  int T;     // threads per transform
+  int M;     // transforms (rows or columns) per CTA
+  int npad;  // shared-memory slots per transform (contiguous layout)
+};
+
+struct FftArgs {
+  PassPlan pp;
+  const void* in;
+  void* out;
+  const void* ker;        // convolution: kernel spectrum
+  const void* tw;         // W_n^k, k in [0, n), compute precision
+  const void* tw2;        // real transforms: W_{2n}^k, k in [0, n]
+  long long ntrans;       // contiguous: number of transforms
+  long long inner;        // strided: number of columns (axis stride in elements)
+  long long outer;        // strided: number of outer batches
+  long long in_bs;        // elements between transforms (contiguous) / outer batches (strided)
+  long long out_bs;
+  long long ker_bs;       // kernel batch stride (0 = one spectrum broadcast to all batches)
+  int col_tiles;          // strided: ceil(inner / M)
+  int sig_lo, sig_hi;     // input positions outside [lo, hi) read as zero
+  double scale;           // applied at the final store
+  int nreal;              // real transforms: logical real length N
+};
+
+// ---------------------------------------------------------------------------
+// thread placement
+// ---------------------------------------------------------------------------
+template <bool STRIDED>
+struct Place {
+  int t, m;
+  bool valid;
+  long long in0, out0, ker0;  // element offset of point 0
+  long long ps;               // point stride in elements
+  __device__ __forceinline__ Place(const FftArgs& a) {
+    const int tid = threadIdx.x;
+    if (STRIDED) {
+      m = tid % a.pp.M;
+      t = tid / a.pp.M;
+      const long long o = blockIdx.x / a.col_tiles;
+      const long long c = (long long)(blockIdx.x % a.col_tiles) * a.pp.M + m;
+      valid = c < a.inner;
+      in0 = o * a.in_bs + c;
+      out0 = o * a.out_bs + c;
+      ker0 = o * a.ker_bs + c;
+      ps = a.inner;
+    } else {
+      t = tid % a.pp.T;
+      m = tid / a.pp.T;
+      const long long g = (long long)blockIdx.x * a.pp.M + m;
+      valid = g < a.ntrans;
+      in0 = g * a.in_bs;
+      out0 = g * a.out_bs;
+      ker0 = g * a.ker_bs;
+      ps = 1;
+    }
+  }
+  // shared-memory slot of point i of this thread's transform
+  __device__ __forceinline__ int sidx(const PassPlan& pp, int i) const {
+    if (STRIDED) return i * pp.M + m;
+    return m * pp.npad + i + (i >> 4);
+  }
+};
+
+template <int V>
+using IC = std::integral_constant<int, V>;
+
+// Runtime radix -> compile-time radix.
+template <class F>
+__device__ __forceinline__ void radix_dispatch(int R, F&& f) {
+  switch (R) {
+    case 1: f(IC<1>{}); break;
+    case 2: f(IC<2>{}); break;
+    case 3: f(IC<3>{}); break;
+    case 4: f(IC<4>{}); break;
+    case 5: f(IC<5>{}); break;
+    case 6: f(IC<6>{}); break;
+    case 7: f(IC<7>{}); break;
+    case 8: f(IC<8>{}); break;
+    case 9: f(IC<9>{}); break;
+    case 10: f(IC<10>{}); break;
+    case 11: f(IC<11>{}); break;
+    case 12: f(IC<12>{}); break;
+    case 13: f(IC<13>{}); break;
+    case 16: f(IC<16>{}); break;
+    default: break;
+  }
+}
+
+// v[b*R + r] <- f(j + r*nb) for the thread's butterflies j = t + b*T < nb
+template <int R, int MAXE, class Re, class F>
+__device__ __forceinline__ void gather(Cx<Re>* v, int nb, int T, int t, F&& f) {
+  constexpr int B = MAXE / R;
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    const int j = t + b * T;
+    if (j < nb) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[b * R + r] = f(j + r * nb);
+    }
+  }
+}
+
+// f(j + r*nb, v[b*R + r]) : natural-order positions (last pass outputs)
+template <int R, int MAXE, class Re, class F>
+__device__ __forceinline__ void each_natural(Cx<Re>* v, int nb, int T, int t, F&& f) {
+  constexpr int B = MAXE / R;
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    const int j = t + b * T;
+    if (j < nb) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) f(j + r * nb, v[b * R + r]);
+    }
+  }
+}
+
+template <int R, int MAXE, bool INV, class Re>
+__device__ __forceinline__ void butterflies(Cx<Re>* v, int nb, int T, int t, int ns, int n, const Cx<Re>* tw) {
+  constexpr int B = MAXE / R;
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    const int j = t + b * T;
+    if (j < nb) {
+      if (ns > 1) {
+        const int k = j % ns;
+        const int step = k * (n / (ns * R));
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          const Cx<Re> w = ldg(&tw[r * step]);
+          v[b * R + r] = INV ? cmulc(v[b * R + r], w) : cmul(v[b * R + r], w);
+        }
+      }
+      Dft<R, INV, Re>::run(&v[b * R]);
+    }
+  }
+}
+
+template <int R, int MAXE, class Re, class G>
+__device__ __forceinline__ void scatter(const Cx<Re>* v, int nb, int T, int t, int ns, G&& g) {
+  constexpr int B = MAXE / R;
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    const int j = t + b * T;
+    if (j < nb) {
+      const int k = j % ns;
+      const int base = (j - k) * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) g(base + r * ns, v[b * R + r]);
+    }
+  }
+}
+
+// Runs every pass on v, which must already hold the inputs of the first
+// executed pass.  reversed = run radices last-to-first.  Returns with v
+// holding natural-order outputs laid out for the last executed radix.
+template <int MAXE, bool INV, bool STRIDED, class Re>
+__device__ __forceinline__ void run_passes(Cx<Re>* v, const PassPlan& pp, bool reversed, const Place<STRIDED>& pl,
+                                           Cx<Re>* sm, const Cx<Re>* tw) {
+  const int n = pp.n, P = pp.npass, T = pp.T, t = pl.t;
+  int ns = 1;
+  for (int q = 0; q < P; ++q) {
+    const int p = reversed ? P - 1 - q : q;
+    const int R = pp.radix[p];
+    radix_dispatch(R, [&](auto rc) {
+      constexpr int RR = decltype(rc)::value;
+      butterflies<RR, MAXE, INV, Re>(v, n / RR, T, t, ns, n, tw);
+    });
+    if (q + 1 < P) {
+      __syncthreads();
+      radix_dispatch(R, [&](auto rc) {
+        constexpr int RR = decltype(rc)::value;
+        scatter<RR, MAXE, Re>(v, n / RR, T, t, ns, [&](int pos, Cx<Re> val) { sm[pl.sidx(pp, pos)] = val; });
+      });
+      __syncthreads();
+      const int R2 = pp.radix[reversed ? P - 2 - q : q + 1];
+      radix_dispatch(R2, [&](auto rc) {
+        constexpr int RR = decltype(rc)::value;
+        gather<RR, MAXE, Re>(v, n / RR, T, t, [&](int pos) { return sm[pl.sidx(pp, pos)]; });
+      });
+    }
+    ns *= R;
+  }
+}
+
+template <class Re>
+__device__ __forceinline__ Cx<Re>* smem_base() {
+  extern __shared__ __align__(16) unsigned char vdx_smem_raw[];
+  return reinterpret_cast<Cx<Re>*>(vdx_smem_raw);
+}
+
+// ---------------------------------------------------------------------------
+// complex-to-complex
+// ---------------------------------------------------------------------------
+template <int MAXE, bool INV, bool STRIDED, class S, class Re>
+__global__ void __launch_bounds__(1024) k_c2c(FftArgs a) {
+  const Place<STRIDED> pl(a);
+  const PassPlan& pp = a.pp;
+  Cx<Re>* sm = smem_base<Re>();
+  const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
+  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
+  S* out = reinterpret_cast<S*>(a.out) + pl.out0;
+  Cx<Re> v[MAXE];
+  const int n = pp.n;
+  const int lo = a.sig_lo, hi = a.sig_hi;
+  radix_dispatch(pp.radix[0], [&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    gather<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos) {
+      if (!pl.valid || pos < lo || pos >= hi) return mk<Re>(Re(0), Re(0));
+      return Conv<S, Re>::ld(in + pos * pl.ps);
+    });
+  });
+  run_passes<MAXE, INV, STRIDED, Re>(v, pp, false, pl, sm, tw);
+  const Re s = Re(a.scale);
+  radix_dispatch(pp.radix[pp.npass - 1], [&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    each_natural<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos, Cx<Re> val) {
+      if (pl.valid) Conv<S, Re>::st(out + pos * pl.ps, scale(val, s));
+    });
+  });
+}
+
+// ---------------------------------------------------------------------------
+// fused convolution: forward FFT -> spectrum * op(kernel) -> inverse FFT
+// kop: 0 = multiply by conj(kernel) (reference default,
+// vkdispatch/fft/shader_factories.py:136-145), 1 = multiply by kernel.
+// ---------------------------------------------------------------------------
+template <int MAXE, bool STRIDED, class S, class K, class Re>
+__global__ void __launch_bounds__(1024) k_conv(FftArgs a, int kop) {
+  const Place<STRIDED> pl(a);
+  const PassPlan& pp = a.pp;
+  Cx<Re>* sm = smem_base<Re>();
+  const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
+  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
+  S* out = reinterpret_cast<S*>(a.out) + pl.out0;
+  const K* ker = reinterpret_cast<const K*>(a.ker) + pl.ker0;
+  Cx<Re> v[MAXE];
+  const int n = pp.n;
+  const int lo = a.sig_lo, hi = a.sig_hi;
+  radix_dispatch(pp.radix[0], [&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    gather<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos) {
+      if (!pl.valid || pos < lo || pos >= hi) return mk<Re>(Re(0), Re(0));
+      return Conv<S, Re>::ld(in + pos * pl.ps);
+    });
+  });
+  run_passes<MAXE, false, STRIDED, Re>(v, pp, false, pl, sm, tw);
+  radix_dispatch(pp.radix[pp.npass - 1], [&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    constexpr int B = MAXE / RR;
+    const int nb = n / RR;
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      const int j = pl.t + b * pp.T;
+      if (j < nb) {
+#pragma unroll
+        for (int r = 0; r < RR; ++r) {
+          const int pos = j + r * nb;
+          Cx<Re> kv = pl.valid ? Conv<K, Re>::ld(ker + pos * pl.ps) : mk<Re>(Re(0), Re(0));
+          v[b * RR + r] = kop == 0 ? cmulc(v[b * RR + r], kv) : cmul(v[b * RR + r], kv);
+        }
+      }
+    }
+  });
+  run_passes<MAXE, true, STRIDED, Re>(v, pp, true, pl, sm, tw);
+  const Re s = Re(a.scale);
+  radix_dispatch(pp.radix[0], [&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    each_natural<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos, Cx<Re> val) {
+      if (pl.valid) Conv<S, Re>::st(out + pos * pl.ps, scale(val, s));
+    });
+  });
+}
+
+// ---------------------------------------------------------------------------
+// real-to-complex, even N = 2n, rows of the packed RFFT layout: row pitch
+// n+1 complex elements = 2n+2 reals (vkdispatch/base/buffer.py:377-448).
+// z[m] = x[2m] + i x[2m+1] -> Z = FFT_n(z) ->
+// X[k] = (Z[k] + conj Z[n-k])/2 - i W_2n^k (Z[k] - conj Z[n-k])/2, k = 0..n
+// ---------------------------------------------------------------------------
+template <int MAXE, class S, class Re>
+__global__ void __launch_bounds__(1024) k_r2c_even(FftArgs a) {
+  using SR = typename RealOf<S>::type;
+  const Place<false> pl(a);
+  const PassPlan& pp = a.pp;
+  Cx<Re>* sm = smem_base<Re>();
+  const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
+  const Cx<Re>* tw2 = reinterpret_cast<const Cx<Re>*>(a.tw2);
+  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
+  const SR* inr = reinterpret_cast<const SR*>(in);
+  S* out = reinterpret_cast<S*>(a.out) + pl.out0;
+  Cx<Re> v[MAXE];
+  const int n = pp.n;
+  const int lo = a.sig_lo, hi = a.sig_hi;
+  const bool full = lo <= 0 && hi >= 2 * n;
+  radix_dispatch(pp.radix[0], [&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    gather<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos) {
+      if (!pl.valid) return mk<Re>(Re(0), Re(0));
+      if (full) return Conv<S, Re>::ld(in + pos);
+      const int e = 2 * pos, o = 2 * pos + 1;
+      Re xr = (e >= lo && e < hi) ? ld_real<Re>(inr + e) : Re(0);
+      Re xi = (o >= lo && o < hi) ? ld_real<Re>(inr + o) : Re(0);
+      return mk<Re>(xr, xi);
+    });
+  });
+  run_passes<MAXE, false, false, Re>(v, pp, false, pl, sm, tw);
+  const int RL = pp.radix[pp.npass - 1];
+  __syncthreads();
+  radix_dispatch(RL, [&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    each_natural<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos, Cx<Re> val) { sm[pl.sidx(pp, pos)] = val; });
+  });
+  __syncthreads();
+  const Re half = Re(0.5);
+  radix_dispatch(RL, [&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    each_natural<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int k, Cx<Re> zk) {
+      const int kc = k == 0 ? 0 : n - k;
+      const Cx<Re> zc = conj(sm[pl.sidx(pp, kc)]);
+      const Cx<Re> e = scale(zk + zc, half);
+      const Cx<Re> d = scale(zk - zc, half);
+      const Cx<Re> o = mk<Re>(d.y, -d.x);  // d / i
+      const Cx<Re> x = e + cmul(ldg(&tw2[k]), o);
+      if (pl.valid) Conv<S, Re>::st(out + k, x);
+    });
+  });
+  if (pl.t == 0 && pl.valid) {
+    const Cx<Re> z0 = sm[pl.sidx(pp, 0)];
+    Conv<S, Re>::st(out + n, mk<Re>(z0.x - z0.y, Re(0)));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// complex-to-real, even N = 2n (Hermitian half X[0..n] -> N reals).
+// Z[k] = (X[k] + conj X[n-k]) + i W_2n^{-k} (X[k] - conj X[n-k]), with the
+// imaginary parts of X[0] and X[n] dropped (the real part of the full-length
+// inverse does not depend on them) -> z = IFFT_n(Z) -> x[2m] + i x[2m+1] = z[m]
+// ---------------------------------------------------------------------------
+template <int MAXE, class S, class Re>
+__global__ void __launch_bounds__(1024) k_c2r_even(FftArgs a) {
+  const Place<false> pl(a);
+  const PassPlan& pp = a.pp;
+  Cx<Re>* sm = smem_base<Re>();
+  const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
+  const Cx<Re>* tw2 = reinterpret_cast<const Cx<Re>*>(a.tw2);
+  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
+  S* out = reinterpret_cast<S*>(a.out) + pl.out0;
+  Cx<Re> v[MAXE];
+  const int n = pp.n;
+  for (int i = pl.t; i <= n; i += pp.T) {
+    Cx<Re> x = pl.valid ? Conv<S, Re>::ld(in + i) : mk<Re>(Re(0), Re(0));
+    if (i == 0 || i == n) x.y = Re(0);
+    sm[pl.sidx(pp, i)] = x;
+  }
+  __syncthreads();
+  radix_dispatch(pp.radix[0], [&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    gather<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int k) {
+      const Cx<Re> xk = sm[pl.sidx(pp, k)];
+      const Cx<Re> xc = conj(sm[pl.sidx(pp, n - k)]);
+      const Cx<Re> s = xk + xc;
+      const Cx<Re> d = xk - xc;
+      const Cx<Re> wd = cmulc(d, ldg(&tw2[k]));  // d * W^{-k}
+      return mk<Re>(s.x - wd.y, s.y + wd.x);      // s + i*wd
+    });
+  });
+  run_passes<MAXE, true, false, Re>(v, pp, false, pl, sm, tw);
+  const Re s = Re(a.scale);
+  radix_dispatch(pp.radix[pp.npass - 1], [&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    each_natural<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos, Cx<Re> val) {
+      if (pl.valid) Conv<S, Re>::st(out + pos, scale(val, s));
+    });
+  });
+}
+
+// ---------------------------------------------------------------------------
+// real transforms of odd length N: full-length complex FFT of the real row
+// (imaginary part zero), keeping bins 0..N/2 (forward), or of the
+// Hermitian-extended half spectrum, keeping real parts (inverse) -- the
+// reference's own R2C I/O rules (vkdispatch/fft/global_memory_iterators.py:
+// 85-92, 214-226).  Row pitch N+1 reals = N/2+1 complex.
+// ---------------------------------------------------------------------------
+template <int MAXE, bool INV, class S, class Re>
+__global__ void __launch_bounds__(1024) k_real_odd(FftArgs a) {
+  using SR = typename RealOf<S>::type;
+  const Place<false> pl(a);
+  const PassPlan& pp = a.pp;
+  Cx<Re>* sm = smem_base<Re>();
+  const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
+  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
+  S* out = reinterpret_cast<S*>(a.out) + pl.out0;
+  Cx<Re> v[MAXE];
+  const int n = pp.n;
+  const int h = n / 2;
+  const int lo = a.sig_lo, hi = a.sig_hi;
+  radix_dispatch(pp.radix[0], [&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    gather<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos) {
+      if (!pl.valid) return mk<Re>(Re(0), Re(0));
+      if (!INV) {
+        if (pos < lo || pos >= hi) return mk<Re>(Re(0), Re(0));
+        return mk<Re>(ld_real<Re>(reinterpret_cast<const SR*>(in) + pos), Re(0));
+      }
+      if (pos <= h) return Conv<S, Re>::ld(in + pos);
+      return conj(Conv<S, Re>::ld(in + (n - pos)));
+    });
+  });
+  run_passes<MAXE, INV, false, Re>(v, pp, false, pl, sm, tw);
+  const Re s = Re(a.scale);
+  radix_dispatch(pp.radix[pp.npass - 1], [&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    each_natural<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos, Cx<Re> val) {
+      if (!pl.valid) return;
+      if (!INV) {
+        if (pos <= h) Conv<S, Re>::st(out + pos, val);
+      } else {
+        st_real<Re>(reinterpret_cast<SR*>(out) + pos, val.x * s);
+      }
+    });
+  });
+}
+
+// ---------------------------------------------------------------------------
+// twiddle tables, built in FP64: tab[k] = exp(-2 pi i k / den), k < count
+// ---------------------------------------------------------------------------
+template <class Re>
+__global__ void k_twiddle(Cx<Re>* tab, int count, int den) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  double s, c;
+  // 2k/den carries one double rounding (relative 2^-53); no range reduction is
+  // needed because k < den
+  sincospi(2.0 * double(k) / double(den), &s, &c);
+  tab[k] = mk<Re>(Re(c), Re(-s));
+}
+
+}  // namespace vdx

@@ -1,0 +1,451 @@
+// C ABI of libvdx: argument validation, the FFT plan builder, twiddle-table
+// cache and kernel dispatch.  See include/vdx.h for the contract.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "vdx.h"
+#include "vdx_internal.h"
+
+using namespace vdx;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(VDX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+
+// ---------------------------------------------------------------------------
+// twiddle tables: one per (device, count, denominator, precision), built once
+// and kept for the life of the process (a few KB each)
+// ---------------------------------------------------------------------------
+std::mutex g_tab_mu;
+std::map<std::tuple<int, int, int, bool>, void*> g_tabs;
+
+int get_table(int dev, int count, int den, bool f64, void** out) {
+  std::lock_guard<std::mutex> lock(g_tab_mu);
+  auto key = std::make_tuple(dev, count, den, f64);
+  auto it = g_tabs.find(key);
+  if (it != g_tabs.end()) {
+    *out = it->second;
+    return VDX_OK;
+  }
+  void* p = nullptr;
+  const size_t bytes = size_t(count) * (f64 ? 16 : 8);
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) return fail(VDX_ERR_NOMEM, std::string("twiddle table allocation: ") + cudaGetErrorString(e));
+  cudaStream_t s;
+  e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(e, "twiddle stream");
+  e = launch_twiddle(p, count, den, f64, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  if (e != cudaSuccess) {
+    cudaFree(p);
+    return cuda_fail(e, "twiddle table build");
+  }
+  g_tabs[key] = p;
+  *out = p;
+  return VDX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// radix factorisation
+// ---------------------------------------------------------------------------
+// Splits n into passes: radix 16 for each 2^4, the leftover power of two
+// folded into an odd radix when possible (6, 10, 12), 9 for pairs of 3s, then
+// 3, 5, 7, 11, 13.  Fails for primes above 13, the reference's largest
+// supported prime (vkdispatch/fft/prime_utils.py:9-10).
+bool factor_radices(int n, int maxe, std::vector<int>& radices, std::string& why) {
+  radices.clear();
+  if (n == 1) {
+    radices.push_back(1);
+    return true;
+  }
+  int m = n, a = 0, cnt[14] = {0};
+  while (m % 2 == 0) {
+    m /= 2;
+    ++a;
+  }
+  for (int p : {3, 5, 7, 11, 13})
+    while (m % p == 0) {
+      m /= p;
+      ++cnt[p];
+    }
+  if (m != 1) {
+    why = "FFT length " + std::to_string(n) + " has a prime factor " + std::to_string(m) +
+          " larger than 13 (supported radices: 2, 3, 5, 7, 11, 13)";
+    return false;
+  }
+  const int big2 = maxe >= 16 ? 16 : 8;
+  const int big2log = big2 == 16 ? 4 : 3;
+  while (a >= big2log) {
+    radices.push_back(big2);
+    a -= big2log;
+  }
+  int rem2 = 1 << a;  // 1, 2, 4 or 8
+  while (cnt[3] >= 2 && maxe >= 9) {
+    radices.push_back(9);
+    cnt[3] -= 2;
+  }
+  if (cnt[3] == 1) {
+    if (rem2 == 2 && maxe >= 6) {
+      radices.push_back(6);
+      rem2 = 1;
+    } else if (rem2 == 4 && maxe >= 12) {
+      radices.push_back(12);
+      rem2 = 1;
+    } else {
+      radices.push_back(3);
+    }
+    cnt[3] = 0;
+  }
+  while (cnt[3] > 0) {
+    radices.push_back(3);
+    --cnt[3];
+  }
+  for (int i = 0; i < cnt[5]; ++i) {
+    if (rem2 == 2 && maxe >= 10) {
+      radices.push_back(10);
+      rem2 = 1;
+    } else {
+      radices.push_back(5);
+    }
+  }
+  for (int p : {7, 11, 13})
+    for (int i = 0; i < cnt[p]; ++i) radices.push_back(p);
+  if (rem2 > 1) radices.push_back(rem2);
+  for (int r : radices)
+    if (r > maxe) {
+      why = "radix " + std::to_string(r) + " exceeds the per-thread register budget";
+      return false;
+    }
+  if ((int)radices.size() > kMaxPasses) {
+    why = "too many radix passes";
+    return false;
+  }
+  std::sort(radices.begin(), radices.end(), [](int x, int y) { return x > y; });
+  return true;
+}
+
+int store_of(int t) {
+  switch (t) {
+    case VDX_C64: return ST_C64;
+    case VDX_C32: return ST_C32;
+    case VDX_C128: return ST_C128;
+    case VDX_BF16X2: return ST_BF16;
+    default: return -1;
+  }
+}
+
+size_t store_bytes(int st) { return st == ST_C128 ? 16 : st == ST_C64 ? 8 : 4; }
+
+}  // namespace
+
+struct vdx_plan {
+  vdx_fft_desc d;
+  int dev;
+  int op;  // vdx::Op
+  bool strided;
+  bool f64;
+  int store;
+  int N;  // axis length (real length for R2C/C2R)
+  FftArgs args;
+  Launch launch;
+  std::vector<int> radices;
+};
+
+extern "C" {
+
+int vdx_version(void) { return 100; }
+
+int vdx_last_error(char* buf, size_t n) {
+  if (!buf || n == 0) return VDX_ERR_INVALID;
+  std::snprintf(buf, n, "%s", g_last_error.c_str());
+  return VDX_OK;
+}
+
+int vdx_device_count(int* count) {
+  if (!count) return fail(VDX_ERR_INVALID, "count is NULL");
+  cudaError_t e = cudaGetDeviceCount(count);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+  return VDX_OK;
+}
+
+int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
+  if (!desc || !plan) return fail(VDX_ERR_INVALID, "desc and plan must be non-NULL");
+  *plan = nullptr;
+  const vdx_fft_desc& d = *desc;
+  if (d.ndim < 1 || d.ndim > 4) return fail(VDX_ERR_INVALID, "ndim must be 1..4");
+  for (int i = 0; i < d.ndim; ++i)
+    if (d.shape[i] < 1) return fail(VDX_ERR_INVALID, "every dimension must be >= 1");
+  if (d.axis < 0 || d.axis >= d.ndim) return fail(VDX_ERR_INVALID, "axis out of range");
+  if (d.kind < VDX_KIND_C2C || d.kind > VDX_KIND_CONV) return fail(VDX_ERR_INVALID, "unknown transform kind");
+  const bool real = d.kind == VDX_KIND_R2C || d.kind == VDX_KIND_C2R;
+  if (real && d.axis != d.ndim - 1)
+    return fail(VDX_ERR_INVALID, "R2C/C2R transforms run on the last (contiguous) axis only");
+
+  const int st = store_of(d.io_type);
+  if (st < 0) return fail(VDX_ERR_INVALID, "io_type must be VDX_C64, VDX_C32, VDX_C128 or VDX_BF16X2");
+  if (d.compute_type != VDX_C64 && d.compute_type != VDX_C128)
+    return fail(VDX_ERR_INVALID, "compute_type must be VDX_C64 or VDX_C128");
+  const bool f64 = d.compute_type == VDX_C128;
+  if (f64 != (st == ST_C128))
+    return fail(VDX_ERR_UNSUPPORTED,
+                "supported (io, compute) pairs: complex64/complex64, complex32/complex64, bf16x2/complex64, "
+                "complex128/complex128");
+  if (d.kind == VDX_KIND_CONV) {
+    if (d.kernel_type != d.io_type) return fail(VDX_ERR_UNSUPPORTED, "kernel_type must equal io_type");
+    if (d.kernel_op != VDX_KOP_MUL_CONJ && d.kernel_op != VDX_KOP_MUL)
+      return fail(VDX_ERR_INVALID, "unknown kernel_op");
+  }
+  if (real && (st == ST_BF16)) return fail(VDX_ERR_UNSUPPORTED, "real transforms support complex64/complex32/complex128");
+
+  long long inner = 1, outer = 1;
+  for (int i = d.axis + 1; i < d.ndim; ++i) inner *= d.shape[i];
+  for (int i = 0; i < d.axis; ++i) outer *= d.shape[i];
+  const long long N64 = d.shape[d.axis];
+  if (N64 > (1 << 24)) return fail(VDX_ERR_UNSUPPORTED, "axis length above 2^24");
+  const int N = (int)N64;
+
+  int lo = 0, hi = N;
+  if (!(d.signal_lo == 0 && (d.signal_hi <= 0 || d.signal_hi == N)) && !(d.signal_lo < 0 && d.signal_hi < 0)) {
+    if (d.signal_lo < 0 || d.signal_hi <= d.signal_lo || d.signal_hi > N)
+      return fail(VDX_ERR_INVALID, "signal range must satisfy 0 <= lo < hi <= N");
+    if (d.kind == VDX_KIND_C2R) return fail(VDX_ERR_UNSUPPORTED, "signal range is defined for forward inputs only");
+    lo = (int)d.signal_lo;
+    hi = (int)d.signal_hi;
+  }
+
+  auto* p = new vdx_plan();
+  p->d = d;
+  p->f64 = f64;
+  p->store = st;
+  p->N = N;
+  cudaError_t e = cudaGetDevice(&p->dev);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(e, "cudaGetDevice");
+  }
+
+  const bool even_real = real && (N % 2 == 0);
+  const int n = even_real ? N / 2 : N;  // complex points per transform
+  const int maxe = f64 ? MaxE<double>::value : MaxE<float>::value;
+  std::string why;
+  if (!factor_radices(n, maxe, p->radices, why)) {
+    delete p;
+    return fail(VDX_ERR_UNSUPPORTED, why);
+  }
+
+  // threads per transform: enough that every pass fits in MAXE registers
+  int T = 1;
+  for (int r : p->radices) {
+    const int nb = n / r;
+    const int per = std::max(1, maxe / r);
+    T = std::max(T, (nb + per - 1) / per);
+  }
+  if (T > 1024) {
+    delete p;
+    return fail(VDX_ERR_UNSUPPORTED, "FFT length " + std::to_string(n) + " needs more than 1024 threads per transform");
+  }
+
+  int smem_optin = 0;
+  cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->dev);
+  if (smem_optin <= 0) smem_optin = 48 * 1024;
+  const size_t cbytes = f64 ? 16 : 8;
+  const bool strided = inner > 1;
+  p->strided = strided;
+  const bool need_smem = p->radices.size() > 1 || even_real;
+  const int npad = n + 1 + ((n + 1) >> 4) + 1;
+
+  int M = 1;
+  size_t smem = 0;
+  if (strided) {
+    M = (int)std::min<long long>(16, inner);
+    M = std::max(1, std::min(M, 1024 / T));
+    while (M > 1 && need_smem && size_t(n) * M * cbytes > size_t(smem_optin)) M /= 2;
+    smem = need_smem ? size_t(n) * M * cbytes : 0;
+  } else {
+    const long long ntrans = outer;
+    M = std::max(1, 256 / T);
+    M = (int)std::min<long long>(M, ntrans);
+    M = std::max(1, std::min(M, 1024 / T));
+    while (M > 1 && need_smem && size_t(npad) * M * cbytes > size_t(smem_optin) / 2) M /= 2;
+    smem = need_smem ? size_t(npad) * M * cbytes : 0;
+  }
+  if (smem > size_t(smem_optin)) {
+    delete p;
+    return fail(VDX_ERR_UNSUPPORTED, "FFT length " + std::to_string(n) + " does not fit in shared memory");
+  }
+
+  FftArgs& a = p->args;
+  std::memset(&a, 0, sizeof(a));
+  a.pp.n = n;
+  a.pp.npass = (int)p->radices.size();
+  for (int i = 0; i < a.pp.npass; ++i) a.pp.radix[i] = p->radices[i];
+  a.pp.T = T;
+  a.pp.M = M;
+  a.pp.npad = npad;
+  a.sig_lo = lo;
+  a.sig_hi = hi;
+  a.nreal = N;
+
+  const bool norm = d.normalize != 0;
+  switch (d.kind) {
+    case VDX_KIND_C2C:
+      p->op = d.inverse ? OP_C2C_INV : OP_C2C_FWD;
+      a.scale = (d.inverse && norm) ? 1.0 / N : 1.0;
+      break;
+    case VDX_KIND_CONV:
+      p->op = OP_CONV;
+      a.scale = norm ? 1.0 / N : 1.0;
+      break;
+    case VDX_KIND_R2C:
+      p->op = even_real ? OP_R2C_EVEN : OP_R2C_ODD;
+      a.scale = 1.0;
+      break;
+    default:
+      p->op = even_real ? OP_C2R_EVEN : OP_C2R_ODD;
+      a.scale = norm ? 1.0 / N : 1.0;
+      break;
+  }
+
+  const long long row = real ? (N / 2 + 1) : N;  // complex elements per row of the buffer
+  if (strided) {
+    a.inner = inner;
+    a.outer = outer;
+    a.in_bs = a.out_bs = (long long)N * inner;
+    a.ker_bs = d.kernel_broadcast ? 0 : (long long)N * inner;
+    a.col_tiles = (int)((inner + M - 1) / M);
+    const long long blocks = outer * a.col_tiles;
+    if (blocks > 0x7fffffffLL) {
+      delete p;
+      return fail(VDX_ERR_UNSUPPORTED, "too many transforms for one launch");
+    }
+    p->launch.grid = dim3((unsigned)blocks);
+  } else {
+    a.ntrans = outer;
+    a.inner = 1;
+    a.in_bs = a.out_bs = row;
+    a.ker_bs = d.kernel_broadcast ? 0 : row;
+    const long long blocks = (outer + M - 1) / M;
+    if (blocks > 0x7fffffffLL) {
+      delete p;
+      return fail(VDX_ERR_UNSUPPORTED, "too many transforms for one launch");
+    }
+    p->launch.grid = dim3((unsigned)blocks);
+  }
+  p->launch.block = dim3(T * M);
+  p->launch.smem = smem;
+
+  void* tw = nullptr;
+  int rc = get_table(p->dev, n, n, f64, &tw);
+  if (rc != VDX_OK) {
+    delete p;
+    return rc;
+  }
+  a.tw = tw;
+  if (even_real) {
+    void* tw2 = nullptr;
+    rc = get_table(p->dev, n + 1, 2 * n, f64, &tw2);
+    if (rc != VDX_OK) {
+      delete p;
+      return rc;
+    }
+    a.tw2 = tw2;
+  }
+  *plan = p;
+  return VDX_OK;
+}
+
+int vdx_fft_plan_destroy(vdx_plan* plan) {
+  delete plan;
+  return VDX_OK;
+}
+
+int vdx_fft_plan_describe(const vdx_plan* p, char* buf, size_t n) {
+  if (!p || !buf || n == 0) return fail(VDX_ERR_INVALID, "plan and buf must be non-NULL");
+  std::string r;
+  for (size_t i = 0; i < p->radices.size(); ++i) r += (i ? "x" : "") + std::to_string(p->radices[i]);
+  static const char* ops[] = {"c2c_fwd", "c2c_inv", "conv", "r2c_even", "c2r_even", "r2c_odd", "c2r_odd"};
+  std::snprintf(buf, n,
+                "{\"op\": \"%s\", \"N\": %d, \"n\": %d, \"radices\": \"%s\", \"threads_per_transform\": %d, "
+                "\"transforms_per_cta\": %d, \"strided\": %s, \"grid\": %u, \"block\": %u, \"smem\": %zu}",
+                ops[p->op], p->N, p->args.pp.n, r.c_str(), p->args.pp.T, p->args.pp.M, p->strided ? "true" : "false",
+                p->launch.grid.x, p->launch.block.x, p->launch.smem);
+  return VDX_OK;
+}
+
+int vdx_fft_exec(const vdx_plan* p, const void* in, void* out, const void* kernel, void* stream) {
+  if (!p) return fail(VDX_ERR_INVALID, "plan is NULL");
+  if (!in || !out) return fail(VDX_ERR_INVALID, "in and out must be non-NULL device pointers");
+  if (p->op == OP_CONV && !kernel) return fail(VDX_ERR_INVALID, "convolution needs a kernel spectrum");
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev != p->dev) return fail(VDX_ERR_INVALID, "plan was created on another device");
+  FftArgs a = p->args;
+  a.in = in;
+  a.out = out;
+  a.ker = kernel;
+  Launch l = p->launch;
+  l.stream = reinterpret_cast<cudaStream_t>(stream);
+  switch (p->store) {
+    case ST_C64: e = launch_fft<Cx<float>, float>(a, l, p->op, p->strided, p->d.kernel_op); break;
+    case ST_C32: e = launch_fft<c32s, float>(a, l, p->op, p->strided, p->d.kernel_op); break;
+    case ST_BF16: e = launch_fft<bf16c, float>(a, l, p->op, p->strided, p->d.kernel_op); break;
+    case ST_C128: e = launch_fft<Cx<double>, double>(a, l, p->op, p->strided, p->d.kernel_op); break;
+    default: return fail(VDX_ERR_INVALID, "bad plan storage type");
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "FFT launch");
+  return VDX_OK;
+}
+
+int vdx_reduce_partial_count(int64_t n, int64_t* partial_count) {
+  if (!partial_count || n < 1) return fail(VDX_ERR_INVALID, "n must be >= 1 and partial_count non-NULL");
+  long long parts = (n + 4095) / 4096;
+  if (parts > 1024) parts = 1024;
+  *partial_count = parts;
+  return VDX_OK;
+}
+
+int vdx_reduce(int op, int map, int in_type, const void* in, int64_t n, int64_t batch, void* out, void* workspace,
+               void* stream) {
+  if (!in || !out || !workspace) return fail(VDX_ERR_INVALID, "in, out and workspace must be non-NULL");
+  if (n < 1 || batch < 1) return fail(VDX_ERR_INVALID, "n and batch must be >= 1");
+  if (batch > 65535) return fail(VDX_ERR_UNSUPPORTED, "batch above 65535 rows");
+  if (op < VDX_RED_ADD || op > VDX_RED_XOR) return fail(VDX_ERR_INVALID, "unknown reduction op");
+  if (map < VDX_MAP_IDENTITY || map > VDX_MAP_SIN) return fail(VDX_ERR_INVALID, "unknown map");
+  const bool integer = in_type == VDX_I32 || in_type == VDX_U32;
+  if (!integer && in_type != VDX_F32 && in_type != VDX_F64 && in_type != VDX_C64)
+    return fail(VDX_ERR_INVALID, "in_type must be F32, F64, C64, I32 or U32");
+  if (op >= VDX_RED_AND && !integer) return fail(VDX_ERR_INVALID, "bitwise reductions need integer input");
+  if (op >= VDX_RED_AND && map != VDX_MAP_IDENTITY) return fail(VDX_ERR_INVALID, "bitwise reductions take no map");
+  if (in_type == VDX_C64 && (map == VDX_MAP_IDENTITY || map == VDX_MAP_SIN))
+    return fail(VDX_ERR_INVALID, "complex input needs a map to a real value (abs, square, real, imag)");
+  if (in_type != VDX_C64 && (map == VDX_MAP_REAL || map == VDX_MAP_IMAG))
+    return fail(VDX_ERR_INVALID, "real/imag maps need complex input");
+  if (integer && map == VDX_MAP_SIN) return fail(VDX_ERR_INVALID, "sin map needs floating-point input");
+  int64_t parts = 0;
+  vdx_reduce_partial_count(n, &parts);
+  cudaError_t e = launch_reduce(op, map, in_type, in, n, batch, out, workspace, (int)parts,
+                                reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "reduce launch");
+  return VDX_OK;
+}
+
+}  // extern "C"

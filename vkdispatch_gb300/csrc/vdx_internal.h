@@ -1,0 +1,64 @@
+// Internal launch interface between the C ABI (vdx_api.cu) and the kernel
+// translation units.  Each launcher picks the template instantiation for a
+// (storage, compute, direction, layout) combination and enqueues it.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fft_kernels.cuh"
+
+namespace vdx {
+
+enum Store { ST_C64 = 0, ST_C32 = 1, ST_C128 = 2, ST_BF16 = 3 };
+
+struct Launch {
+  dim3 grid;
+  dim3 block;
+  size_t smem;
+  cudaStream_t stream;
+};
+
+// Elements per thread of the instantiated kernels: registers hold MAXE
+// complex values of the current pass, and every radix used by a plan must be
+// <= MAXE.  fp32 compute keeps 16 (32 registers of data under the 64-register
+// cap of 1024-thread CTAs); fp64 compute keeps 8.
+template <class Re>
+struct MaxE;
+template <>
+struct MaxE<float> {
+  static constexpr int value = 16;
+};
+template <>
+struct MaxE<double> {
+  static constexpr int value = 8;
+};
+
+// Supported (storage, compute) pairs: complex64/fp32, complex32/fp32,
+// bf16x2/fp32, complex128/fp64.
+enum Op { OP_C2C_FWD, OP_C2C_INV, OP_CONV, OP_R2C_EVEN, OP_C2R_EVEN, OP_R2C_ODD, OP_C2R_ODD };
+
+template <class S, class Re>
+cudaError_t launch_fft(const FftArgs& a, const Launch& l, int op, bool strided, int kop);
+
+cudaError_t launch_twiddle(void* tab, int count, int den, bool f64, cudaStream_t s);
+
+// Opt a kernel into more than 48 KB of dynamic shared memory once.
+template <class K>
+inline cudaError_t prepare_smem(K kernel, size_t smem) {
+  if (smem <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+template <class K, class... Args>
+inline cudaError_t enqueue(K kernel, const Launch& l, Args... args) {
+  cudaError_t e = prepare_smem(kernel, l.smem);
+  if (e != cudaSuccess) return e;
+  kernel<<<l.grid, l.block, l.smem, l.stream>>>(args...);
+  return cudaGetLastError();
+}
+
+// reductions
+cudaError_t launch_reduce(int op, int map, int in_type, const void* in, long long n, long long batch, void* out,
+                          void* partials, int nparts, cudaStream_t s);
+
+}  // namespace vdx

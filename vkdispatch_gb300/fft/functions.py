@@ -1,0 +1,381 @@
+"""Public FFT API with the reference's signatures and semantics
+(vkdispatch/fft/functions.py:104-713): in-place transforms on Buffers,
+per-axis passes for 2-D / 3-D, packed real transforms on RFFTBuffers, and
+fused convolutions that multiply by the conjugate kernel spectrum.
+
+Each call resolves precisions (vkdispatch/fft/precision.py:67-99), fetches a
+cached plan and records one launch into the graph (immediate by default).
+"""
+
+from __future__ import annotations
+
+from typing import Optional, Tuple, Union
+
+import numpy as np
+
+from .. import _lib as L
+from .. import dtype as dt
+from .. import graph as G
+from ..buffer import Buffer, RFFTBuffer
+from . import plan as P
+
+_PRECISION_ORDER = (dt.complex32, dt.complex64, dt.complex128)
+
+
+def _validate_complex(t, arg: str) -> None:
+    if t not in _PRECISION_ORDER and t != dt.complexbf16:
+        raise ValueError(f"{arg} must be one of complex32, complex64, or complex128 (got {t})")
+
+
+def resolve_compute_precision(io_types, compute_type: Optional[dt.dtype]) -> dt.dtype:
+    """Reference rule: explicit compute_type wins; otherwise the widest I/O
+    precision, at least complex64."""
+    if compute_type is not None:
+        _validate_complex(compute_type, "compute_type")
+        return compute_type
+    if not io_types:
+        return dt.complex64
+    for t in io_types:
+        _validate_complex(t, "io_precision")
+    rank = max(_PRECISION_ORDER.index(t) if t in _PRECISION_ORDER else 0 for t in io_types)
+    return _PRECISION_ORDER[max(rank, 1)]
+
+
+def _compute_code(io_type: dt.dtype, compute: dt.dtype) -> int:
+    # complex32 compute runs with fp32 butterflies (never less accurate than asked)
+    if compute in (dt.complex32, dt.complex64, dt.complexbf16):
+        return L.VDX_C64
+    return L.VDX_C128
+
+
+def _norm_axis(axis: Optional[int], ndim: int) -> int:
+    if axis is None:
+        return ndim - 1
+    if axis < 0:
+        axis += ndim
+    if not 0 <= axis < ndim:
+        raise ValueError(f"axis {axis} out of range for {ndim} dimensions")
+    return axis
+
+
+def _no_maps(**maps) -> None:
+    for name, m in maps.items():
+        if m is not None:
+            raise NotImplementedError(
+                f"{name} is not in the supported map menu of this build (use the io/compute dtype arguments, "
+                "input_signal_range, or kernel_inner_only instead)"
+            )
+
+
+def _signal(sr, N: int) -> Optional[Tuple[int, int]]:
+    if sr is None:
+        return None
+    lo, hi = sr
+    lo = 0 if lo is None else int(lo)
+    hi = N if hi is None else int(hi)
+    if lo == 0 and hi == N:
+        return None
+    return (lo, hi)
+
+
+def _record(graph, launch, keep=()) -> None:
+    G.resolve(graph).record(launch, keep)
+
+
+def fft(
+    *buffers: Buffer,
+    buffer_shape: Tuple = None,
+    graph: G.CommandGraph = None,
+    print_shader: bool = False,
+    axis: int = None,
+    name: str = None,
+    inverse: bool = False,
+    normalize_inverse: bool = True,
+    r2c: bool = False,
+    input_map=None,
+    output_map=None,
+    output_type: dt.dtype = None,
+    input_type: dt.dtype = None,
+    compute_type: dt.dtype = None,
+    input_signal_range: Union[Tuple[Optional[int], Optional[int]], None] = None,
+):
+    if len(buffers) < 1:
+        raise ValueError("At least one buffer must be provided")
+    if input_map is None and output_map is None and len(buffers) != 1:
+        raise ValueError("fft() expects exactly one buffer unless input_map/output_map are used")
+    _no_maps(input_map=input_map, output_map=output_map)
+    buf = buffers[0]
+    if buffer_shape is None:
+        buffer_shape = buf.shape
+    buffer_shape = tuple(int(s) for s in buffer_shape)
+    out_t = buf.var_type if output_type is None else output_type
+    _validate_complex(out_t, "output_type")
+    in_t = out_t if input_type is None else input_type
+    _validate_complex(in_t, "input_type")
+    if in_t != out_t:
+        raise ValueError("input_type must match output_type when input_map is None (default FFT path is in-place)")
+    if out_t != buf.var_type:
+        raise ValueError(f"output_type {out_t.name} does not match the buffer type {buf.var_type.name}")
+    compute = resolve_compute_precision([out_t, in_t], compute_type)
+    ax = _norm_axis(axis, len(buffer_shape))
+    N = buffer_shape[ax]
+    if r2c:
+        if ax != len(buffer_shape) - 1:
+            raise ValueError("R2C io only supported for contiguous data")
+        expect = buffer_shape[:-1] + (buffer_shape[-1] // 2 + 1,)
+        if tuple(buf.shape) != expect:
+            raise ValueError(f"R2C buffer of shape {buf.shape} does not match real shape {buffer_shape}")
+        kind = L.VDX_KIND_C2R if inverse else L.VDX_KIND_R2C
+    else:
+        if int(np.prod(buffer_shape)) > buf.size:
+            raise ValueError(f"buffer_shape {buffer_shape} exceeds the buffer size {buf.size}")
+        kind = L.VDX_KIND_C2C
+    plan = P.get_plan(
+        buffer_shape,
+        ax,
+        kind,
+        inverse,
+        normalize_inverse,
+        out_t.vdx_code,
+        _compute_code(out_t, compute),
+        _signal(input_signal_range, N),
+    )
+    if print_shader:
+        print(plan.describe())
+    ptr = buf.ptr
+    _record(graph, lambda s: plan.exec(ptr, ptr, None, s), (buf,))
+
+
+def fft2(buffer: Buffer, graph=None, print_shader=False, input_map=None, output_map=None, output_type=None,
+         input_type=None, compute_type=None):
+    if len(buffer.shape) not in (2, 3):
+        raise ValueError("Buffer must have 2 or 3 dimensions")
+    kw = dict(graph=graph, print_shader=print_shader, output_type=output_type, input_type=input_type,
+              compute_type=compute_type)
+    fft(buffer, axis=len(buffer.shape) - 2, input_map=input_map, **kw)
+    fft(buffer, axis=len(buffer.shape) - 1, output_map=output_map, **kw)
+
+
+def fft3(buffer: Buffer, graph=None, print_shader=False, input_map=None, output_map=None, output_type=None,
+         input_type=None, compute_type=None):
+    if len(buffer.shape) != 3:
+        raise ValueError("Buffer must have 3 dimensions")
+    kw = dict(graph=graph, print_shader=print_shader, output_type=output_type, input_type=input_type,
+              compute_type=compute_type)
+    fft(buffer, axis=0, input_map=input_map, **kw)
+    fft(buffer, axis=1, **kw)
+    fft(buffer, axis=2, output_map=output_map, **kw)
+
+
+def ifft(buffer: Buffer, graph=None, print_shader=False, axis=None, name=None, normalize=True, input_map=None,
+         output_map=None, output_type=None, input_type=None, compute_type=None):
+    fft(buffer, graph=graph, print_shader=print_shader, axis=axis, name=name, inverse=True,
+        normalize_inverse=normalize, input_map=input_map, output_map=output_map, output_type=output_type,
+        input_type=input_type, compute_type=compute_type)
+
+
+def ifft2(buffer: Buffer, graph=None, print_shader=False, normalize=True, input_map=None, output_map=None,
+          output_type=None, input_type=None, compute_type=None):
+    if len(buffer.shape) not in (2, 3):
+        raise ValueError("Buffer must have 2 or 3 dimensions")
+    kw = dict(graph=graph, print_shader=print_shader, normalize=normalize, output_type=output_type,
+              input_type=input_type, compute_type=compute_type)
+    ifft(buffer, axis=len(buffer.shape) - 2, input_map=input_map, **kw)
+    ifft(buffer, axis=len(buffer.shape) - 1, output_map=output_map, **kw)
+
+
+def ifft3(buffer: Buffer, graph=None, print_shader=False, normalize=True, input_map=None, output_map=None,
+          output_type=None, input_type=None, compute_type=None):
+    if len(buffer.shape) != 3:
+        raise ValueError("Buffer must have 3 dimensions")
+    kw = dict(graph=graph, print_shader=print_shader, normalize=normalize, output_type=output_type,
+              input_type=input_type, compute_type=compute_type)
+    ifft(buffer, axis=0, input_map=input_map, **kw)
+    ifft(buffer, axis=1, **kw)
+    ifft(buffer, axis=2, output_map=output_map, **kw)
+
+
+def rfft(buffer: RFFTBuffer, graph=None, print_shader=False, name=None, compute_type=None):
+    fft(buffer, buffer_shape=buffer.real_shape, graph=graph, print_shader=print_shader, name=name, r2c=True,
+        output_type=buffer.var_type, input_type=buffer.var_type, compute_type=compute_type)
+
+
+def rfft2(buffer: RFFTBuffer, graph=None, print_shader=False, compute_type=None):
+    if len(buffer.real_shape) not in (2, 3):
+        raise ValueError("Buffer must have 2 or 3 dimensions")
+    rfft(buffer, graph=graph, print_shader=print_shader, compute_type=compute_type)
+    fft(buffer, graph=graph, print_shader=print_shader, axis=len(buffer.real_shape) - 2,
+        output_type=buffer.var_type, input_type=buffer.var_type, compute_type=compute_type)
+
+
+def rfft3(buffer: RFFTBuffer, graph=None, print_shader=False, compute_type=None):
+    if len(buffer.real_shape) != 3:
+        raise ValueError("Buffer must have 3 dimensions")
+    rfft(buffer, graph=graph, print_shader=print_shader, compute_type=compute_type)
+    for ax in (1, 0):
+        fft(buffer, graph=graph, print_shader=print_shader, axis=ax, output_type=buffer.var_type,
+            input_type=buffer.var_type, compute_type=compute_type)
+
+
+def irfft(buffer: RFFTBuffer, graph=None, print_shader=False, name=None, normalize=True, compute_type=None):
+    fft(buffer, buffer_shape=buffer.real_shape, graph=graph, print_shader=print_shader, name=name, inverse=True,
+        normalize_inverse=normalize, r2c=True, output_type=buffer.var_type, input_type=buffer.var_type,
+        compute_type=compute_type)
+
+
+def irfft2(buffer: RFFTBuffer, graph=None, print_shader=False, normalize=True, compute_type=None):
+    if len(buffer.real_shape) not in (2, 3):
+        raise ValueError("Buffer must have 2 or 3 dimensions")
+    ifft(buffer, graph=graph, print_shader=print_shader, axis=len(buffer.real_shape) - 2, normalize=normalize,
+         output_type=buffer.var_type, input_type=buffer.var_type, compute_type=compute_type)
+    irfft(buffer, graph=graph, print_shader=print_shader, normalize=normalize, compute_type=compute_type)
+
+
+def irfft3(buffer: RFFTBuffer, graph=None, print_shader=False, normalize=True, compute_type=None):
+    if len(buffer.real_shape) != 3:
+        raise ValueError("Buffer must have 3 dimensions")
+    for ax in (0, 1):
+        ifft(buffer, graph=graph, print_shader=print_shader, axis=ax, normalize=normalize,
+             output_type=buffer.var_type, input_type=buffer.var_type, compute_type=compute_type)
+    irfft(buffer, graph=graph, print_shader=print_shader, normalize=normalize, compute_type=compute_type)
+
+
+def convolve(
+    *buffers: Buffer,
+    kernel_map=None,
+    kernel_num: int = 1,
+    buffer_shape: Tuple = None,
+    graph: G.CommandGraph = None,
+    print_shader: bool = False,
+    axis: int = None,
+    normalize: bool = True,
+    name: str = None,
+    transposed_kernel: bool = False,
+    kernel_inner_only: bool = False,
+    input_map=None,
+    output_map=None,
+    output_type: dt.dtype = None,
+    input_type: dt.dtype = None,
+    kernel_type: dt.dtype = None,
+    compute_type: dt.dtype = None,
+    input_signal_range=None,
+):
+    """In-place FFT -> spectrum * conj(kernel) -> inverse FFT along `axis`, in
+    one kernel.  The kernel spectrum is read at the signal's own index
+    (vkdispatch/fft/io_manager.py:181-187), or from one slab shared by all
+    outer batches when kernel_inner_only is set (or when the kernel buffer
+    holds exactly one slab)."""
+    if len(buffers) < 1:
+        raise ValueError("At least one buffer must be provided")
+    if kernel_map is None and len(buffers) < 2:
+        raise ValueError("convolve() requires at least an output buffer and kernel buffer")
+    _no_maps(input_map=input_map, output_map=output_map, kernel_map=kernel_map)
+    if kernel_num != 1:
+        raise NotImplementedError("kernel_num > 1 is not supported by this build")
+    buf, ker = buffers[0], buffers[1]
+    if buffer_shape is None:
+        buffer_shape = buf.shape
+    buffer_shape = tuple(int(s) for s in buffer_shape)
+    out_t = buf.var_type if output_type is None else output_type
+    in_t = out_t if input_type is None else input_type
+    k_t = ker.var_type if kernel_type is None else kernel_type
+    for t, nm in ((out_t, "output_type"), (in_t, "input_type"), (k_t, "kernel_type")):
+        _validate_complex(t, nm)
+    if in_t != out_t:
+        raise ValueError("input_type must match output_type when input_map is None (default FFT path is in-place)")
+    if k_t != ker.var_type or out_t != buf.var_type:
+        raise ValueError("kernel_type/output_type must match the buffers' types")
+    compute = resolve_compute_precision([out_t, in_t, k_t], compute_type)
+    ax = _norm_axis(axis, len(buffer_shape))
+    total = int(np.prod(buffer_shape))
+    slab = int(np.prod(buffer_shape[ax:]))
+    broadcast = bool(kernel_inner_only)
+    if not broadcast and ker.size < total:
+        if ker.size >= slab:
+            broadcast = True
+        else:
+            raise ValueError(f"kernel buffer of {ker.size} elements is smaller than the signal ({total})")
+    plan = P.get_plan(
+        buffer_shape,
+        ax,
+        L.VDX_KIND_CONV,
+        False,
+        normalize,
+        out_t.vdx_code,
+        _compute_code(out_t, compute),
+        _signal(input_signal_range, buffer_shape[ax]),
+        L.VDX_KOP_MUL_CONJ,
+        k_t.vdx_code,
+        broadcast,
+    )
+    if print_shader:
+        print(plan.describe())
+    ptr, kptr = buf.ptr, ker.ptr
+    _record(graph, lambda s: plan.exec(ptr, ptr, kptr, s), (buf, ker))
+
+
+def convolve2D(buffer: Buffer, kernel: Buffer, kernel_map=None, buffer_shape=None, graph=None, print_shader=False,
+               normalize=True, transposed_kernel=False, kernel_inner_only=False, input_map=None, output_map=None,
+               output_type=None, input_type=None, kernel_type=None, compute_type=None):
+    if len(buffer.shape) not in (2, 3):
+        raise ValueError("Buffer must have 2 or 3 dimensions")
+    fft(buffer, graph=graph, print_shader=print_shader, input_map=input_map, output_type=output_type,
+        input_type=input_type, compute_type=compute_type)
+    convolve(buffer, kernel, kernel_map=kernel_map, buffer_shape=buffer_shape, graph=graph,
+             transposed_kernel=transposed_kernel, kernel_inner_only=kernel_inner_only, print_shader=print_shader,
+             axis=len(buffer.shape) - 2, normalize=normalize, output_type=output_type, input_type=input_type,
+             kernel_type=kernel_type, compute_type=compute_type)
+    ifft(buffer, graph=graph, print_shader=print_shader, normalize=normalize, output_map=output_map,
+         output_type=output_type if output_map is None else None,
+         input_type=input_type if output_map is None else None, compute_type=compute_type)
+
+
+def convolve2DR(buffer: RFFTBuffer, kernel: RFFTBuffer, kernel_map=None, buffer_shape=None, transposed_kernel=False,
+                kernel_inner_only=False, graph=None, print_shader=False, normalize=True, compute_type=None):
+    if len(buffer.real_shape) not in (2, 3):
+        raise ValueError("Buffer must have 2 or 3 dimensions")
+    rfft(buffer, graph=graph, print_shader=print_shader, compute_type=compute_type)
+    convolve(buffer, kernel, kernel_map=kernel_map, buffer_shape=buffer_shape, graph=graph,
+             transposed_kernel=transposed_kernel, kernel_inner_only=kernel_inner_only, print_shader=print_shader,
+             axis=len(buffer.shape) - 2, normalize=normalize, output_type=buffer.var_type,
+             input_type=buffer.var_type, kernel_type=kernel.var_type, compute_type=compute_type)
+    irfft(buffer, graph=graph, print_shader=print_shader, normalize=normalize, compute_type=compute_type)
+
+
+def get_transposed_size(buffer_shape: Tuple, axis: int = None, compute_type=dt.complex64) -> int:
+    """Elements of the kernel layout that ``transpose`` produces.  This build
+    reads kernel spectra in natural order, so the layout is the spectrum
+    itself."""
+    return int(np.prod(buffer_shape))
+
+
+def transpose(in_buffer: Buffer, conv_shape: Tuple = None, axis: int = None, out_buffer: Buffer = None,
+              graph=None, kernel_inner_only: bool = False, print_shader: bool = False, input_type=None,
+              output_type=None, compute_type=None) -> Buffer:
+    """Re-lays a kernel spectrum for ``convolve(..., transposed_kernel=True)``
+    (vkdispatch/fft/functions.py:648-713).  The fused kernels here read the
+    spectrum in natural order, so this is an ordered copy into out_buffer."""
+    import torch
+
+    size = get_transposed_size(tuple(in_buffer.shape), axis)
+    out_t = (out_buffer.var_type if out_buffer is not None else in_buffer.var_type) if output_type is None else output_type
+    if out_buffer is None:
+        out_buffer = Buffer((size,), out_t)
+    if out_buffer.var_type != out_t:
+        raise ValueError(f"out_buffer type ({out_buffer.var_type.name}) does not match output_type ({out_t.name})")
+    if out_buffer.size < size:
+        raise ValueError(f"Output buffer size {out_buffer.size} is smaller than expected transposed size {size}")
+    src, dst = in_buffer, out_buffer
+
+    def launch(stream):
+        s = torch.cuda.ExternalStream(stream) if stream else torch.cuda.current_stream()
+        with torch.cuda.stream(s):
+            n = src.tensor.numel()
+            dst.tensor.reshape(-1)[:n].copy_(src.tensor.reshape(-1), non_blocking=True)
+
+    _record(graph, launch, (src, dst))
+    return out_buffer
+
+
+def cache_clear() -> None:
+    P.cache_clear()

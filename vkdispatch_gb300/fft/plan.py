@@ -1,0 +1,93 @@
+"""FFT plan cache over the C ABI (the role of the reference's lru_cache'd
+kernel factories, vkdispatch/fft/shader_factories.py:11, 107)."""
+
+from __future__ import annotations
+
+import ctypes
+import json
+import threading
+from typing import Dict, Optional, Tuple
+
+import torch
+
+from .. import _lib as L
+
+_cache: Dict[tuple, "Plan"] = {}
+_mu = threading.Lock()
+
+
+class Plan:
+    def __init__(self, desc: L.FftDesc):
+        self.desc = desc
+        h = ctypes.c_void_p()
+        L.check(L.lib().vdx_fft_plan_create(ctypes.byref(desc), ctypes.byref(h)), "FFT plan")
+        self.handle = h
+
+    def describe(self) -> dict:
+        buf = ctypes.create_string_buffer(1024)
+        L.check(L.lib().vdx_fft_plan_describe(self.handle, buf, len(buf)), "FFT plan describe")
+        return json.loads(buf.value.decode())
+
+    def exec(self, in_ptr: int, out_ptr: int, ker_ptr: Optional[int], stream: int) -> None:
+        L.check(L.lib().vdx_fft_exec(self.handle, in_ptr, out_ptr, ker_ptr, stream), "FFT exec")
+
+    def __del__(self):
+        try:
+            if self.handle:
+                L.lib().vdx_fft_plan_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def get_plan(
+    shape: Tuple[int, ...],
+    axis: int,
+    kind: int,
+    inverse: bool,
+    normalize: bool,
+    io_type: int,
+    compute_type: int,
+    signal_range: Optional[Tuple[int, int]] = None,
+    kernel_op: int = L.VDX_KOP_MUL_CONJ,
+    kernel_type: Optional[int] = None,
+    kernel_broadcast: bool = False,
+) -> Plan:
+    dev = torch.cuda.current_device()
+    key = (dev, tuple(shape), axis, kind, bool(inverse), bool(normalize), io_type, compute_type, signal_range,
+           kernel_op, kernel_type, bool(kernel_broadcast))
+    p = _cache.get(key)
+    if p is not None:
+        return p
+    with _mu:
+        p = _cache.get(key)
+        if p is not None:
+            return p
+        d = L.FftDesc()
+        d.ndim = len(shape)
+        for i, s in enumerate(shape):
+            d.shape[i] = int(s)
+        d.axis = axis
+        d.kind = kind
+        d.inverse = int(bool(inverse))
+        d.normalize = int(bool(normalize))
+        d.io_type = io_type
+        d.compute_type = compute_type
+        if signal_range is None:
+            d.signal_lo, d.signal_hi = -1, -1
+        else:
+            d.signal_lo, d.signal_hi = int(signal_range[0]), int(signal_range[1])
+        d.kernel_op = kernel_op
+        d.kernel_type = io_type if kernel_type is None else kernel_type
+        d.kernel_broadcast = int(bool(kernel_broadcast))
+        p = Plan(d)
+        _cache[key] = p
+        return p
+
+
+def cache_clear() -> None:
+    with _mu:
+        _cache.clear()
+
+
+def cache_info() -> int:
+    return len(_cache)

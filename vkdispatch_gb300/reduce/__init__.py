@@ -1,0 +1,212 @@
+"""vd.reduce-compatible map-reduce API (vkdispatch/reduce/decorator.py:22-64,
+operations.py:17-66, reduce_function.py:73-162).
+
+``@reduce(identity)`` and ``@map_reduce(op)`` return a ReduceFunction whose
+call enqueues the two libvdx reduction launches and returns a new Buffer in
+the reference's layout: shape ``(parts + 1[, batch])`` with the results in
+the first ``batch`` elements (``res.read(0)[0]`` for one row) and the
+stage-1 partials after them.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import inspect
+from typing import List, Optional, Union
+
+import numpy as np
+
+from .. import _lib as L
+from .. import codegen as vc
+from .. import dtype as dt
+from .. import graph as G
+from ..buffer import Buffer
+
+
+@dataclasses.dataclass
+class ReduceOp:
+    name: str
+    code: int
+    identity: Union[int, float, str]
+
+
+SubgroupAdd = ReduceOp("add", L.VDX_RED_ADD, 0)
+SubgroupMul = ReduceOp("mul", L.VDX_RED_MUL, 1)
+SubgroupMin = ReduceOp("min", L.VDX_RED_MIN, "inf")
+SubgroupMax = ReduceOp("max", L.VDX_RED_MAX, "-inf")
+SubgroupAnd = ReduceOp("and", L.VDX_RED_AND, -1)
+SubgroupOr = ReduceOp("or", L.VDX_RED_OR, 0)
+SubgroupXor = ReduceOp("xor", L.VDX_RED_XOR, 0)
+
+_OPS = {"add": SubgroupAdd, "mul": SubgroupMul, "min": SubgroupMin, "max": SubgroupMax, "and": SubgroupAnd,
+        "or": SubgroupOr, "xor": SubgroupXor}
+
+mapped_io_index = vc.mapped_io_index
+
+
+def _trace_reduction(func) -> ReduceOp:
+    a, b = vc.Sym("a"), vc.Sym("b")
+    try:
+        r = func(a, b)
+    except Exception as e:  # noqa: BLE001
+        raise NotImplementedError(f"reduction {func.__name__} could not be traced: {e}") from e
+    if isinstance(r, vc.Sym) and r.op in _OPS and len(r.args) == 2:
+        ids = {x.op if isinstance(x, vc.Sym) else None for x in r.args}
+        if ids == {"a", "b"}:
+            return _OPS[r.op]
+    raise NotImplementedError(f"reduction {func.__name__} is not one of add, mul, min, max, and, or, xor")
+
+
+def _trace_map(func, in_types) -> int:
+    bufs = [vc.SymBuffer(i, t) for i, t in enumerate(in_types)]
+    try:
+        r = func(*bufs)
+    except Exception as e:  # noqa: BLE001
+        raise NotImplementedError(f"map {func.__name__} could not be traced: {e}") from e
+
+    def is_load(x):
+        return isinstance(x, vc.Sym) and x.op == "load" and x.args == (0,)
+
+    if len(in_types) != 1:
+        raise NotImplementedError(f"map {func.__name__}: maps over more than one buffer are not in the menu")
+    if is_load(r):
+        return L.VDX_MAP_IDENTITY
+    if isinstance(r, vc.Sym):
+        if r.op == "sin" and is_load(r.args[0]):
+            return L.VDX_MAP_SIN
+        if r.op in ("abs", "length") and is_load(r.args[0]):
+            return L.VDX_MAP_ABS
+        if r.op == "mul" and is_load(r.args[0]) and is_load(r.args[1]):
+            return L.VDX_MAP_SQUARE
+        if r.op == "real" and is_load(r.args[0]):
+            return L.VDX_MAP_REAL
+        if r.op == "imag" and is_load(r.args[0]):
+            return L.VDX_MAP_IMAG
+        if r.op == "sqrt":  # sqrt(re*re + im*im)
+            s = r.args[0]
+            if isinstance(s, vc.Sym) and s.op == "add":
+                parts = {p.args[0].op if isinstance(p, vc.Sym) and p.op == "mul" and isinstance(p.args[0], vc.Sym)
+                         else None for p in s.args}
+                if parts == {"real", "imag"}:
+                    return L.VDX_MAP_ABS
+        if r.op == "add" and all(isinstance(p, vc.Sym) and p.op == "mul" for p in r.args):
+            ops = {p.args[0].op for p in r.args if isinstance(p.args[0], vc.Sym)}
+            if ops == {"real", "imag"}:
+                return L.VDX_MAP_SQUARE
+    raise NotImplementedError(f"map {func.__name__} ({r!r}) is not in the supported map menu")
+
+
+class MappingFunction:
+    """The reference's vd.map object: a function plus its buffer types."""
+
+    def __init__(self, func, return_type=None, input_types=None):
+        self.func = func
+        sig = inspect.signature(func)
+        if return_type is None and sig.return_annotation is not inspect.Parameter.empty:
+            return_type = sig.return_annotation
+        self.return_type = return_type
+        if input_types is None:
+            input_types = [p.annotation for p in sig.parameters.values()]
+        self.buffer_types = list(input_types)
+
+    def input_dtypes(self) -> List[dt.dtype]:
+        out = []
+        for t in self.buffer_types:
+            if hasattr(t, "var_type"):
+                out.append(t.var_type)
+            elif hasattr(t, "__args__"):
+                out.append(t.__args__[0])
+            else:
+                raise ValueError(f"map argument annotation {t} is not a Buffer[...] type")
+        return out
+
+
+def map(func=None, return_type=None, input_types=None):  # noqa: A001 - mirrors vd.map
+    if func is None:
+        return lambda f: MappingFunction(f, return_type, input_types)
+    return MappingFunction(func, return_type, input_types)
+
+
+class ReduceFunction:
+    def __init__(self, reduction: ReduceOp, group_size: Optional[int] = None, axes: Optional[List[int]] = None,
+                 mapping_function: Optional[MappingFunction] = None):
+        self.reduction = reduction
+        self.group_size = group_size
+        self.axes = axes
+        self.map_func = mapping_function
+        self.out_type = mapping_function.return_type if mapping_function is not None else None
+        self._map_code = None
+
+    def _resolve_map(self, in_type: dt.dtype) -> int:
+        if self.map_func is None:
+            return L.VDX_MAP_IDENTITY
+        if self._map_code is None:
+            self._map_code = _trace_map(self.map_func.func, self.map_func.input_dtypes())
+        return self._map_code
+
+    def __call__(self, *args, graph: Optional[G.CommandGraph] = None, **kwargs) -> Buffer:
+        src = args[0]
+        in_type = src.var_type
+        if in_type.vdx_code is None or in_type.vdx_code in (L.VDX_C32, L.VDX_C128, L.VDX_BF16X2):
+            raise NotImplementedError(f"reductions over {in_type.name} buffers are not in the supported menu")
+        map_code = self._resolve_map(in_type)
+        if self.axes is None:
+            n, batch = src.size, 1
+        else:
+            shape = src.shape
+            batched = []
+            for i in range(len(shape)):
+                if i in self.axes:
+                    break
+                batched.append(i)
+            skipped = []
+            for i in range(len(shape) - 1, -1, -1):
+                if i in self.axes:
+                    break
+                skipped.append(i)
+            if skipped:
+                raise ValueError("Reduction axes must be contiguous!")
+            batch = int(np.prod([shape[i] for i in batched])) if batched else 1
+            n = src.size // batch
+        out_code = in_type.vdx_code
+        out_type = in_type
+        if in_type == dt.complex64:
+            out_code, out_type = L.VDX_F32, dt.float32
+        if self.out_type is not None and self.out_type != out_type:
+            raise NotImplementedError(f"map return type {self.out_type} does not match the reduction type {out_type}")
+        parts = ctypes.c_int64()
+        L.check(L.lib().vdx_reduce_partial_count(n, ctypes.byref(parts)), "reduce")
+        shape = (int(parts.value) + 1,) + ((batch,) if batch > 1 else ())
+        res = Buffer(shape, out_type)
+        op = self.reduction.code
+        in_code = in_type.vdx_code
+        ptr, out = src.ptr, res.ptr
+        ws = out + batch * out_type.item_size
+
+        def launch(stream):
+            L.check(L.lib().vdx_reduce(op, map_code, in_code, ptr, n, batch, out, ws, stream), "reduce")
+
+        G.resolve(graph).record(launch, (src, res))
+        return res
+
+
+def reduce(identity, axes=None, group_size=None, mapping_function: MappingFunction = None):
+    def decorator(func):
+        sig = inspect.signature(func)
+        if sig.return_annotation is inspect.Parameter.empty:
+            raise ValueError("Return type must be annotated")
+        op = _trace_reduction(func)
+        mf = mapping_function
+        if mf is not None and mf.return_type != sig.return_annotation:
+            raise ValueError("Mapping function return type must match the return type of the reduction function")
+        return ReduceFunction(op, group_size=group_size, axes=axes, mapping_function=mf)
+
+    return decorator
+
+
+def map_reduce(reduction: ReduceOp, axes=None, group_size=None):
+    def decorator(func):
+        return ReduceFunction(reduction, group_size=group_size, axes=axes, mapping_function=MappingFunction(func))
+
+    return decorator
