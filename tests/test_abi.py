@@ -1,0 +1,100 @@
+"""CPU tests of the C ABI boundary: libvdx.so loads, exports every entry
+point include/vdx.h declares, constants and struct layout agree with the
+Python binding, and host-side validation rejects bad arguments before any
+CUDA call."""
+
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from vkdispatch_gb300 import _lib as L
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "vdx.h"
+
+
+def _declared():
+    src = HEADER.read_text()
+    return sorted(set(re.findall(r"^int\s+(vdx_\w+)\s*\(", src, flags=re.M)))
+
+
+def _defines():
+    src = HEADER.read_text()
+    return {m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+(VDX_\w+)\s+(\d+)", src)}
+
+
+def test_library_exports_every_declared_symbol():
+    lib = L.lib()
+    names = _declared()
+    assert len(names) >= 9
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(names) <= set(L.EXPORTED) | {n for n in names if hasattr(lib, n)}
+
+
+def test_constants_match_header():
+    d = _defines()
+    for k, v in d.items():
+        if hasattr(L, k):
+            assert getattr(L, k) == v, k
+
+
+def test_desc_struct_layout():
+    # int32 ndim, int64 shape[4], int32 axis..compute_type, int64 lo, hi, 4 x int32
+    assert ctypes.sizeof(L.FftDesc) == 8 + 32 + 5 * 4 + 4 + 16 + 16
+    assert L.FftDesc.shape.offset == 8
+    assert L.FftDesc.signal_lo.offset == 64
+
+
+def test_version_and_last_error():
+    lib = L.lib()
+    assert lib.vdx_version() >= 100
+    rc = lib.vdx_fft_plan_create(None, None)
+    assert rc == L.VDX_ERR_INVALID
+    assert "non-NULL" in L.last_error()
+
+
+@pytest.mark.parametrize(
+    "field,value",
+    [("ndim", 0), ("ndim", 5), ("axis", 3), ("kind", 9), ("io_type", 7), ("compute_type", 4)],
+)
+def test_plan_validation_without_gpu(field, value):
+    d = L.FftDesc()
+    d.ndim = 2
+    d.shape[0], d.shape[1] = 4, 64
+    d.axis = 1
+    d.io_type = L.VDX_C64
+    d.compute_type = L.VDX_C64
+    d.signal_lo = d.signal_hi = -1
+    setattr(d, field, value)
+    h = ctypes.c_void_p()
+    rc = L.lib().vdx_fft_plan_create(ctypes.byref(d), ctypes.byref(h))
+    assert rc == L.VDX_ERR_INVALID
+    assert not h.value
+    with pytest.raises(ValueError):
+        L.check(rc, "plan")
+
+
+def test_real_transform_needs_last_axis():
+    d = L.FftDesc()
+    d.ndim = 2
+    d.shape[0], d.shape[1] = 4, 64
+    d.axis = 0
+    d.kind = L.VDX_KIND_R2C
+    d.io_type = d.compute_type = L.VDX_C64
+    h = ctypes.c_void_p()
+    assert L.lib().vdx_fft_plan_create(ctypes.byref(d), ctypes.byref(h)) == L.VDX_ERR_INVALID
+    assert "last" in L.last_error()
+
+
+def test_reduce_validation_without_gpu():
+    lib = L.lib()
+    parts = ctypes.c_int64()
+    assert lib.vdx_reduce_partial_count(300000, ctypes.byref(parts)) == 0
+    assert 1 <= parts.value <= 1024
+    # bitwise op on floats is rejected before any launch
+    rc = lib.vdx_reduce(L.VDX_RED_XOR, 0, L.VDX_F32, 1, 10, 1, 1, 1, None)
+    assert rc == L.VDX_ERR_INVALID
+    rc = lib.vdx_reduce(L.VDX_RED_ADD, L.VDX_MAP_IDENTITY, L.VDX_C64, 1, 10, 1, 1, 1, None)
+    assert rc == L.VDX_ERR_INVALID and "map" in L.last_error()

@@ -1,0 +1,105 @@
+"""CPU tests of host-side logic: map and reduction tracing against the
+functor menu, precision resolution, graph recording."""
+
+import pytest
+
+import vkdispatch_gb300 as vd
+from vkdispatch_gb300 import _lib as L
+from vkdispatch_gb300 import codegen as vc
+from vkdispatch_gb300.codegen import Buff, c64, f32, i32
+from vkdispatch_gb300.reduce import _trace_map, _trace_reduction
+
+
+def test_reduction_tracing():
+    def add(a: f32, b: f32) -> f32:
+        return a + b
+
+    def mn(a: f32, b: f32) -> f32:
+        return vc.min(a, b)
+
+    def x(a: i32, b: i32) -> i32:
+        return a ^ b
+
+    assert _trace_reduction(add).code == L.VDX_RED_ADD
+    assert _trace_reduction(mn).code == L.VDX_RED_MIN
+    assert _trace_reduction(x).code == L.VDX_RED_XOR
+
+    def weird(a: f32, b: f32) -> f32:
+        return a + b + a
+
+    with pytest.raises(NotImplementedError):
+        _trace_reduction(weird)
+
+
+def test_map_tracing_menu():
+    idx = vd.reduce.mapped_io_index
+
+    def ident(b: Buff[f32]) -> f32:
+        return b[idx()]
+
+    def sn(b: Buff[f32]) -> f32:
+        return vc.sin(b[idx()])
+
+    def mag(b: Buff[c64]) -> f32:
+        v = b[idx()]
+        return vc.sqrt(v.real * v.real + v.imag * v.imag)
+
+    def mag2(b: Buff[c64]) -> f32:
+        v = b[idx()]
+        return v.real * v.real + v.imag * v.imag
+
+    def two(b: Buff[f32], c: Buff[f32]) -> f32:
+        return b[idx()] + c[idx()]
+
+    assert _trace_map(ident, [f32]) == L.VDX_MAP_IDENTITY
+    assert _trace_map(sn, [f32]) == L.VDX_MAP_SIN
+    assert _trace_map(mag, [c64]) == L.VDX_MAP_ABS
+    assert _trace_map(mag2, [c64]) == L.VDX_MAP_SQUARE
+    with pytest.raises(NotImplementedError):
+        _trace_map(two, [f32, f32])
+
+
+def test_reduce_decorator_needs_annotation():
+    with pytest.raises(ValueError):
+
+        @vd.reduce.reduce(0)
+        def f(a, b):
+            return a + b
+
+
+def test_precision_resolution():
+    r = vd.fft.resolve_compute_precision
+    assert r([vd.complex32], None) == vd.complex64
+    assert r([vd.complex64, vd.complex32], None) == vd.complex64
+    assert r([vd.complex128, vd.complex64], None) == vd.complex128
+    assert r([vd.complex64], vd.complex128) == vd.complex128
+    with pytest.raises(ValueError):
+        r([vd.float32], None)
+
+
+def test_command_graph_records_and_replays_in_order():
+    g = vd.CommandGraph()
+    seen = []
+    g.record(lambda s: seen.append(("a", s)))
+    g.record(lambda s: seen.append(("b", s)))
+    g.submit(stream=123)
+    g.submit(instance_count=2, stream=7)
+    assert seen == [("a", 123), ("b", 123), ("a", 7), ("b", 7), ("a", 7), ("b", 7)]
+
+
+def test_cuda_graph_capture_routes_stream():
+    from vkdispatch_gb300 import graph as G
+
+    with G.cuda_graph_capture(stream=4242):
+        assert G.current_stream_handle() == 4242
+        with G.suspend_cuda_capture():
+            assert G._tls.stream is None
+
+
+def test_global_graph_swap():
+    g = vd.CommandGraph()
+    old = vd.set_global_graph(g)
+    try:
+        assert vd.global_graph() is g
+    finally:
+        vd.set_global_graph(old)
