@@ -1,0 +1,494 @@
+"""Benchmark: 2-D FFT convolution throughput (GB/s of compulsory HBM traffic).
+
+Workload (the reference's convolve2DR path, vkdispatch/fft/functions.py:614-646):
+64 real 512x512 float32 images, U[-1, 1] from seed 1, convolved with a
+31x31 normalised Gaussian (sigma = 5) placed at [0:31, 0:31] of a zero
+512x512 image; kernel spectrum K = rfft2(kernel) computed on the device and
+replicated to (64, 512, 257) complex64, as the reference's convolve reads the
+kernel at the signal's own index.  One step = rfft (last axis) -> fused
+convolve along axis 1 (FFT, * conj(K), inverse FFT, 1/N) -> irfft, in place on
+one RFFTBuffer: three libvdx launches.
+
+Algorithmic bytes per step (read every input and write every output once per
+pass): rfft 64 MiB + 67,371,008 B; convolve 3 x 67,371,008 B; irfft
+67,371,008 B + 64 MiB = 471,072,768 B.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the CPU restatement of the reference algorithm
+(oracle/vdx_ref.c, all host threads) on a bounded sample of the workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+B, H, W = 64, 512, 512
+KS, SIGMA = 31, 5.0
+HC = W // 2 + 1
+REAL_BYTES = B * H * W * 4  # 67,108,864
+SPEC_BYTES = B * H * HC * 8  # 67,371,008
+ALG_BYTES = {
+    "r2c": REAL_BYTES + SPEC_BYTES,
+    "conv": 3 * SPEC_BYTES,
+    "c2r": SPEC_BYTES + REAL_BYTES,
+}
+STEP_BYTES = sum(ALG_BYTES.values())  # 471,072,768
+METRIC = "2-D FFT convolution throughput (convolve2DR, compulsory HBM bytes / time)"
+WORKLOAD = ("convolve2DR: 64 x 512x512 f32 images U[-1,1] seed 1, 31x31 Gaussian sigma=5 kernel, "
+            "K-hat replicated to 64x512x257 complex64; rfft -> fused conv axis 1 -> irfft, in place")
+
+
+def make_inputs():
+    rng = np.random.default_rng(1)
+    images = rng.uniform(-1.0, 1.0, (B, H, W)).astype(np.float32)
+    ax = np.arange(KS) - KS // 2
+    g = np.exp(-(ax[:, None] ** 2 + ax[None, :] ** 2) / (2 * SIGMA**2))
+    g = g / g.sum()
+    kernel = np.zeros((H, W), np.float32)
+    kernel[:KS, :KS] = g.astype(np.float32)
+    return images, kernel
+
+
+def reference_fp64(images, kernel):
+    """FP64 oracle of one step with the reference's conj(K) convention."""
+    s = np.fft.rfft2(images.astype(np.float64))
+    k = np.fft.rfft2(kernel.astype(np.float64))
+    return np.fft.irfft2(s * np.conj(k), s=(H, W))
+
+
+def _load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _load_traffic(kernel_name):
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    v = d.get(kernel_name)
+    return None if v is None else float(v)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_ours(args):
+    import torch
+
+    import vkdispatch_gb300 as vd
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    images, kernel = make_inputs()
+    # kernel spectrum: rfft2 on the device through the API (tests/test_conv.py:148 flow), replicated
+    kb = vd.asrfftbuffer(kernel)
+    vd.fft.rfft2(kb)
+    kspec = vd.RFFTBuffer((B, H, W))
+    kspec.tensor.copy_(kb.tensor.unsqueeze(0).expand(B, H, HC))
+    buf = vd.RFFTBuffer((B, H, W))
+    buf.write_real(images)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    # correctness of one step against the FP64 oracle
+    vd.fft.convolve2DR(buf, kspec)
+    got = buf.read_real(0)
+    ref = reference_fp64(images, kernel)
+    err = float(np.linalg.norm((got - ref).ravel()) / np.linalg.norm(ref.ravel()))
+
+    def step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        vd.fft.rfft(buf)
+        if ev is not None:
+            ev[1].record(stream)
+        vd.fft.convolve(buf, kspec, axis=1, output_type=buf.var_type, input_type=buf.var_type,
+                        kernel_type=kspec.var_type)
+        if ev is not None:
+            ev[2].record(stream)
+        vd.fft.irfft(buf)
+        if ev is not None:
+            ev[3].record(stream)
+
+    buf.write_real(images)
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+
+    K = args.steps
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(K)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(K):
+        flush.zero_()
+        step(evs[i])
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    per = {"r2c": [], "conv": [], "c2r": []}
+    steps_ms = []
+    for e in evs:
+        per["r2c"].append(e[0].elapsed_time(e[1]))
+        per["conv"].append(e[1].elapsed_time(e[2]))
+        per["c2r"].append(e[2].elapsed_time(e[3]))
+        steps_ms.append(e[0].elapsed_time(e[3]))
+    ms = statistics.mean(steps_ms)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * STEP_BYTES / (ms * 1e-3) / 1e9
+
+    # dominant kernel roofline
+    mean_k = {k: statistics.mean(v) for k, v in per.items()}
+    dom = max(mean_k, key=mean_k.get)
+    peak, peak_kind = _load_peaks()
+    achieved = ALG_BYTES[dom] / (mean_k[dom] * 1e-3) / 1e9
+    traffic = _load_traffic({"r2c": "k_r2c_even", "conv": "k_conv", "c2r": "k_c2r_even"}[dom])
+
+    # end to end through the public API with pinned host buffers
+    h_in = torch.from_numpy(images).pin_memory()
+    h_out = torch.empty((B, H, W), dtype=torch.float32).pin_memory()
+    real_view = torch.view_as_real(buf.tensor).reshape(B, H, 2 * HC)[..., :W]
+    for _ in range(max(1, args.warmup // 2)):
+        real_view.copy_(h_in, non_blocking=True)
+        vd.fft.convolve2DR(buf, kspec)
+        h_out.copy_(real_view, non_blocking=True)
+    torch.cuda.synchronize()
+    e_s = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    KE = max(3, K // 4)
+    e_s[0].record(stream)
+    for _ in range(KE):
+        real_view.copy_(h_in, non_blocking=True)
+        vd.fft.convolve2DR(buf, kspec)
+        h_out.copy_(real_view, non_blocking=True)
+    e_s[1].record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e_s[0].elapsed_time(e_s[1]) / KE
+    e2e_err = float(np.linalg.norm((h_out.numpy() - ref).ravel()) / np.linalg.norm(ref.ravel()))
+
+    extra = cfg1_numbers(vd, torch, flush, args) if rank == 0 and not args.quick else {}
+    cpu = cpu_baseline(images, kernel) if (rank == 0 and not args.quick) else None
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": round(value, 2),
+            "unit": "GB/s",
+            "n_gpus": world,
+            "steps": K,
+            "warmup": args.warmup,
+            "ms_per_step": round(ms, 5),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic (seeded images and Gaussian kernel, the workload's shapes and distributions)",
+            "config": {
+                "workload": WORKLOAD,
+                "algorithmic_bytes_per_step": STEP_BYTES,
+                "l2": "flushed before every step (256 MiB device write, outside the step events)",
+                "parallelism": "replicas" if world > 1 else "single GPU",
+                "error_rel_l2_vs_fp64": err,
+                "per_kernel_ms": {k: round(v, 5) for k, v in mean_k.items()},
+                "wall_s_timed_region": round(wall, 4),
+            },
+            "roofline": {
+                "kernel": dom,
+                "bound": "hbm",
+                "achieved": round(achieved, 1),
+                "peak": peak,
+                "unit": "GB/s",
+                "frac": round(achieved / peak, 4),
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+                "traffic": traffic,
+                "algorithmic_bytes": ALG_BYTES[dom],
+            },
+            "cpu_baseline": cpu,
+            "e2e": {
+                "value": round(world * STEP_BYTES / (e2e_ms * 1e-3) / 1e9, 2),
+                "unit": "GB/s",
+                "ms_per_step": round(e2e_ms, 4),
+                "h2d_bytes_per_step": REAL_BYTES,
+                "d2h_bytes_per_step": REAL_BYTES,
+                "error_rel_l2_vs_fp64": e2e_err,
+            },
+            "gpu_launches": 3 * K,
+            "clocks": clk,
+            "extra": extra,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def cfg1_numbers(vd, torch, flush, args):
+    """Plain batched C2C (N=1024): the 2 MiB case (fwd + inv + magnitude sum)
+    and the HBM-scale variant (batch 262,144 = 2 GiB, L2 flushed)."""
+    out = {}
+    rng = np.random.default_rng(0)
+    x = (rng.standard_normal((256, 1024)) + 1j * rng.standard_normal((256, 1024))).astype(np.complex64)
+    b = vd.asbuffer(x)
+
+    @vd.reduce.map_reduce(vd.reduce.SubgroupAdd)
+    def mag(buffer: vd.codegen.Buff[vd.complex64]) -> vd.float32:
+        v = buffer[vd.reduce.mapped_io_index()]
+        return vd.codegen.sqrt(v.real * v.real + v.imag * v.imag)
+
+    def small_step():
+        vd.fft.fft(b)
+        vd.fft.ifft(b)
+        return mag(b)
+
+    for _ in range(5):
+        small_step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = 200
+    e0.record()
+    for _ in range(n):
+        r = small_step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n
+    s = float(r.read(0)[0])
+    out["cfg1_256x1024_fwd_inv_magsum"] = {"ms_per_step": round(ms, 5),
+                                           "GBps": round(10485760 / (ms * 1e-3) / 1e9, 1),
+                                           "magnitude_sum": s, "launches_per_step": 4}
+
+    big = torch.empty((262144, 1024), dtype=torch.complex64, device="cuda")
+    big.normal_()
+    bb = vd.from_cuda_array(big)
+    peak, _ = _load_peaks()
+    res = {}
+    for name, fn in (("fwd", lambda: vd.fft.fft(bb)), ("inv", lambda: vd.fft.ifft(bb))):
+        for _ in range(3):
+            fn()
+        ts = []
+        for _ in range(10):
+            flush.zero_()
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        t = statistics.median(ts)
+        gbps = 2 * big.numel() * 8 / (t * 1e-3) / 1e9
+        res[name] = {"ms": round(t, 4), "GBps": round(gbps, 1), "frac_of_measured_hbm": round(gbps / peak, 4)}
+    out["cfg1_hbm_1024x262144"] = res
+    del big
+    return out
+
+
+def cpu_baseline(images, kernel, budget_s=8.0):
+    """The CPU restatement of the reference algorithm (oracle/vdx_ref.c, OpenMP
+    over all host threads) on a bounded sample of the workload: as many whole
+    images as fit the time budget."""
+    from oracle import ref
+
+    kp = ref.packed_from_real(kernel)
+    kspec = ref.fft(ref.rfft_packed(kp, W), axis=0)
+    nimg = 1
+    t = 0.0
+    while True:
+        t0 = time.perf_counter()
+        ref.convolve2DR(images[:nimg], kspec)
+        t = time.perf_counter() - t0
+        if t > budget_s / 4 or nimg >= B:
+            break
+        nimg = min(B, nimg * 2)
+    reps = max(1, int(budget_s / max(t, 1e-3) / 2))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ref.convolve2DR(images[:nimg], kspec)
+    t = (time.perf_counter() - t0) / reps
+    sample_bytes = STEP_BYTES * nimg / B
+    return {"value": round(sample_bytes / t / 1e9, 4), "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{nimg} of 64 images per step, {reps} steps (oracle/vdx_ref.c, OpenMP)",
+            "ms_per_image": round(t / nimg * 1e3, 3)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import ref
+
+    images, kernel = make_inputs()
+    kp = ref.packed_from_real(kernel)
+    kspec = ref.fft(ref.rfft_packed(kp, W), axis=0)
+    nimg = 4  # bounded sample of the workload per step
+    kspec = np.ascontiguousarray(np.broadcast_to(kspec, (nimg,) + kspec.shape))  # replicated, as on the GPU
+    for _ in range(max(1, args.warmup)):
+        ref.convolve2DR(images[:nimg], kspec)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ref.convolve2DR(images[:nimg], kspec)
+        ts.append(time.perf_counter() - t0)
+    t = statistics.mean(ts)
+    value = STEP_BYTES * nimg / B / t / 1e9
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": round(value, 4),
+        "unit": "GB/s",
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(t * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded images and Gaussian kernel)",
+        "config": {"workload": WORKLOAD, "sample": f"{nimg} of 64 images per step",
+                   "implementation": "CPU restatement of the reference algorithm (oracle/vdx_ref.c), "
+                                     "bit-exact with the reference's generated kernels on the golden vectors; "
+                                     "the reference's own CPU path (Vulkan on lavapipe) is unavailable on this box"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": cores, "kind": "port",
+                         "sample": f"{nimg} of 64 images per step"},
+        "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_profile(args):
+    """Small fixed cases for ncu captures: a few launches of one workload,
+    no timing.  conv2d = the benchmark step; c2c1024 = 32768 transforms of
+    1024 points (256 MiB, above L2)."""
+    import torch
+
+    import vkdispatch_gb300 as vd
+
+    torch.cuda.set_device(0)
+    if args.profile == "conv2d":
+        images, kernel = make_inputs()
+        kb = vd.asrfftbuffer(kernel)
+        vd.fft.rfft2(kb)
+        kspec = vd.RFFTBuffer((B, H, W))
+        kspec.tensor.copy_(kb.tensor.unsqueeze(0).expand(B, H, HC))
+        buf = vd.RFFTBuffer((B, H, W))
+        buf.write_real(images)
+        for _ in range(args.steps):
+            vd.fft.convolve2DR(buf, kspec)
+    else:
+        n = int(args.profile[3:])
+        x = torch.randn((32 * 1024 * 1024) // n, n, dtype=torch.complex64, device="cuda")
+        b = vd.from_cuda_array(x)
+        for _ in range(args.steps):
+            vd.fft.fft(b)
+            vd.fft.ifft(b)
+    torch.cuda.synchronize()
+    print("profile case done", flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="skip the extra configs and the CPU baseline")
+    ap.add_argument("--profile", default=None, help="run a small case for ncu: conv2d or c2c<N>")
+    args = ap.parse_args()
+    if args.profile:
+        run_profile(args)
+        return
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -103,3 +103,34 @@ def test_global_graph_swap():
         assert vd.global_graph() is g
     finally:
         vd.set_global_graph(old)
+
+
+def test_string_annotations_resolve():
+    ns = {}
+    exec(
+        "from __future__ import annotations\n"
+        "import vkdispatch_gb300 as vd\n"
+        "def m(b: vd.codegen.Buff[vd.complex64]) -> vd.float32:\n"
+        "    v = b[vd.reduce.mapped_io_index()]\n"
+        "    return vd.codegen.sqrt(v.real * v.real + v.imag * v.imag)\n",
+        ns,
+    )
+    mf = vd.reduce.MappingFunction(ns["m"])
+    assert mf.input_dtypes() == [vd.complex64]
+    assert mf.return_type == vd.float32
+
+
+def test_string_annotations_of_enclosing_locals_resolve_by_name():
+    ns = {}
+    exec(
+        "from __future__ import annotations\n"
+        "def outer():\n"
+        "    import vkdispatch_gb300 as vdl\n"
+        "    def m(b: vdl.codegen.Buff[vdl.complex64]) -> vdl.float32:\n"
+        "        return b[0]\n"
+        "    return m\n",
+        ns,
+    )
+    mf = vd.reduce.MappingFunction(ns["outer"]())
+    assert mf.input_dtypes() == [vd.complex64]
+    assert mf.return_type == vd.float32

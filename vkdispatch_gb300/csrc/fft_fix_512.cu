@@ -1,0 +1,6 @@
+// complex64 FFT kernels specialised for n = 512.
+#include "fft_launch.cuh"
+
+namespace vdx {
+template cudaError_t launch_fixed_c64<512>(const FftArgs&, const Launch&, int, bool, int);
+}  // namespace vdx

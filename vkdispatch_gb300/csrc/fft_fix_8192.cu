@@ -1,0 +1,6 @@
+// complex64 FFT kernels specialised for n = 8192.
+#include "fft_launch.cuh"
+
+namespace vdx {
+template cudaError_t launch_fixed_c64<8192>(const FftArgs&, const Launch&, int, bool, int);
+}  // namespace vdx

@@ -62,7 +62,7 @@ struct Place {
   bool valid;
   long long in0, out0, ker0;  // element offset of point 0
   long long ps;               // point stride in elements
-  __device__ __forceinline__ Place(const FftArgs& a) {
+  __device__ __forceinline__ Place(const FftArgs& a, int T) {
     const int tid = threadIdx.x;
     if (STRIDED) {
       m = tid % a.pp.M;
@@ -75,8 +75,8 @@ struct Place {
       ker0 = o * a.ker_bs + c;
       ps = a.inner;
     } else {
-      t = tid % a.pp.T;
-      m = tid / a.pp.T;
+      t = tid % T;
+      m = tid / T;
       const long long g = (long long)blockIdx.x * a.pp.M + m;
       valid = g < a.ntrans;
       in0 = g * a.in_bs;
@@ -213,6 +213,105 @@ __device__ __forceinline__ void run_passes(Cx<Re>* v, const PassPlan& pp, bool r
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// plan policies: how the kernels below learn n, T and the radix passes.
+//   DynPlan   - runtime pass list (any 13-smooth length), radix by switch
+//   FixPlan   - compile-time length, threads per transform and radix list;
+//               every index, division and twiddle stride folds at compile time
+// ---------------------------------------------------------------------------
+template <int... Rs>
+struct RList {};
+
+template <class L>
+struct RFirst;
+template <int R0, int... Rs>
+struct RFirst<RList<R0, Rs...>> {
+  static constexpr int value = R0;
+};
+template <class L>
+struct RLast;
+template <int R0>
+struct RLast<RList<R0>> {
+  static constexpr int value = R0;
+};
+template <int R0, int R1, int... Rs>
+struct RLast<RList<R0, R1, Rs...>> {
+  static constexpr int value = RLast<RList<R1, Rs...>>::value;
+};
+template <class In, class Out = RList<>>
+struct RRev;
+template <int R0, int... Rs, int... Os>
+struct RRev<RList<R0, Rs...>, RList<Os...>> : RRev<RList<Rs...>, RList<R0, Os...>> {};
+template <int... Os>
+struct RRev<RList<>, RList<Os...>> {
+  using type = RList<Os...>;
+};
+
+template <int MAXE_>
+struct DynPlan {
+  static constexpr int MAXE = MAXE_;
+  const PassPlan& pp;
+  __device__ __forceinline__ explicit DynPlan(const PassPlan& p) : pp(p) {}
+  __device__ __forceinline__ int n() const { return pp.n; }
+  __device__ __forceinline__ int T() const { return pp.T; }
+  // radix of the first executed pass (REV: passes run last-to-first)
+  template <bool REV, class F>
+  __device__ __forceinline__ void first(F&& f) const {
+    radix_dispatch(pp.radix[REV ? pp.npass - 1 : 0], f);
+  }
+  template <bool REV, class F>
+  __device__ __forceinline__ void last(F&& f) const {
+    radix_dispatch(pp.radix[REV ? 0 : pp.npass - 1], f);
+  }
+  template <bool INV, bool REV, bool STRIDED, class Re>
+  __device__ __forceinline__ void run(Cx<Re>* v, const Place<STRIDED>& pl, Cx<Re>* sm, const Cx<Re>* tw) const {
+    run_passes<MAXE, INV, STRIDED, Re>(v, pp, REV, pl, sm, tw);
+  }
+};
+
+template <int N, int T, int MAXE, bool INV, class Re, bool STRIDED, int NS, int R, int... Rest>
+__device__ __forceinline__ void chain(Cx<Re>* v, const PassPlan& pp, const Place<STRIDED>& pl, Cx<Re>* sm,
+                                      const Cx<Re>* tw) {
+  butterflies<R, MAXE, INV, Re>(v, N / R, T, pl.t, NS, N, tw);
+  if constexpr (sizeof...(Rest) > 0) {
+    __syncthreads();
+    scatter<R, MAXE, Re>(v, N / R, T, pl.t, NS, [&](int pos, Cx<Re> val) { sm[pl.sidx(pp, pos)] = val; });
+    __syncthreads();
+    constexpr int R2 = RFirst<RList<Rest...>>::value;
+    gather<R2, MAXE, Re>(v, N / R2, T, pl.t, [&](int pos) { return sm[pl.sidx(pp, pos)]; });
+    chain<N, T, MAXE, INV, Re, STRIDED, NS * R, Rest...>(v, pp, pl, sm, tw);
+  }
+}
+
+template <int N, int T, int MAXE, bool INV, class Re, bool STRIDED, int... Rs>
+__device__ __forceinline__ void chain_list(RList<Rs...>, Cx<Re>* v, const PassPlan& pp, const Place<STRIDED>& pl,
+                                           Cx<Re>* sm, const Cx<Re>* tw) {
+  chain<N, T, MAXE, INV, Re, STRIDED, 1, Rs...>(v, pp, pl, sm, tw);
+}
+
+template <int N_, int T_, class L>
+struct FixPlan {
+  static constexpr int MAXE = 16;
+  const PassPlan& pp;
+  __device__ __forceinline__ explicit FixPlan(const PassPlan& p) : pp(p) {}
+  __device__ __forceinline__ static constexpr int n() { return N_; }
+  __device__ __forceinline__ static constexpr int T() { return T_; }
+  template <bool REV, class F>
+  __device__ __forceinline__ void first(F&& f) const {
+    f(IC<REV ? RLast<L>::value : RFirst<L>::value>{});
+  }
+  template <bool REV, class F>
+  __device__ __forceinline__ void last(F&& f) const {
+    f(IC<REV ? RFirst<L>::value : RLast<L>::value>{});
+  }
+  template <bool INV, bool REV, bool STRIDED, class Re>
+  __device__ __forceinline__ void run(Cx<Re>* v, const Place<STRIDED>& pl, Cx<Re>* sm, const Cx<Re>* tw) const {
+    using Order = typename std::conditional<REV, typename RRev<L>::type, L>::type;
+    chain_list<N_, T_, MAXE, INV, Re, STRIDED>(Order{}, v, pp, pl, sm, tw);
+  }
+};
+
 template <class Re>
 __device__ __forceinline__ Cx<Re>* smem_base() {
   extern __shared__ __align__(16) unsigned char vdx_smem_raw[];
@@ -222,29 +321,30 @@ __device__ __forceinline__ Cx<Re>* smem_base() {
 // ---------------------------------------------------------------------------
 // complex-to-complex
 // ---------------------------------------------------------------------------
-template <int MAXE, bool INV, bool STRIDED, class S, class Re>
+template <class Plan, bool INV, bool STRIDED, class S, class Re>
 __global__ void __launch_bounds__(1024) k_c2c(FftArgs a) {
-  const Place<STRIDED> pl(a);
-  const PassPlan& pp = a.pp;
+  const Plan P(a.pp);
+  constexpr int MAXE = Plan::MAXE;
+  const Place<STRIDED> pl(a, P.T());
   Cx<Re>* sm = smem_base<Re>();
   const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
   const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
   S* out = reinterpret_cast<S*>(a.out) + pl.out0;
   Cx<Re> v[MAXE];
-  const int n = pp.n;
+  const int n = P.n();
   const int lo = a.sig_lo, hi = a.sig_hi;
-  radix_dispatch(pp.radix[0], [&](auto rc) {
+  P.template first<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
-    gather<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos) {
+    gather<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos) {
       if (!pl.valid || pos < lo || pos >= hi) return mk<Re>(Re(0), Re(0));
       return Conv<S, Re>::ld(in + pos * pl.ps);
     });
   });
-  run_passes<MAXE, INV, STRIDED, Re>(v, pp, false, pl, sm, tw);
+  P.template run<INV, false>(v, pl, sm, tw);
   const Re s = Re(a.scale);
-  radix_dispatch(pp.radix[pp.npass - 1], [&](auto rc) {
+  P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
-    each_natural<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos, Cx<Re> val) {
+    each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos, Cx<Re> val) {
       if (pl.valid) Conv<S, Re>::st(out + pos * pl.ps, scale(val, s));
     });
   });
@@ -255,33 +355,34 @@ __global__ void __launch_bounds__(1024) k_c2c(FftArgs a) {
 // kop: 0 = multiply by conj(kernel) (reference default,
 // vkdispatch/fft/shader_factories.py:136-145), 1 = multiply by kernel.
 // ---------------------------------------------------------------------------
-template <int MAXE, bool STRIDED, class S, class K, class Re>
+template <class Plan, bool STRIDED, class S, class K, class Re>
 __global__ void __launch_bounds__(1024) k_conv(FftArgs a, int kop) {
-  const Place<STRIDED> pl(a);
-  const PassPlan& pp = a.pp;
+  const Plan P(a.pp);
+  constexpr int MAXE = Plan::MAXE;
+  const Place<STRIDED> pl(a, P.T());
   Cx<Re>* sm = smem_base<Re>();
   const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
   const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
   S* out = reinterpret_cast<S*>(a.out) + pl.out0;
   const K* ker = reinterpret_cast<const K*>(a.ker) + pl.ker0;
   Cx<Re> v[MAXE];
-  const int n = pp.n;
+  const int n = P.n();
   const int lo = a.sig_lo, hi = a.sig_hi;
-  radix_dispatch(pp.radix[0], [&](auto rc) {
+  P.template first<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
-    gather<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos) {
+    gather<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos) {
       if (!pl.valid || pos < lo || pos >= hi) return mk<Re>(Re(0), Re(0));
       return Conv<S, Re>::ld(in + pos * pl.ps);
     });
   });
-  run_passes<MAXE, false, STRIDED, Re>(v, pp, false, pl, sm, tw);
-  radix_dispatch(pp.radix[pp.npass - 1], [&](auto rc) {
+  P.template run<false, false>(v, pl, sm, tw);
+  P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
     constexpr int B = MAXE / RR;
     const int nb = n / RR;
 #pragma unroll
     for (int b = 0; b < B; ++b) {
-      const int j = pl.t + b * pp.T;
+      const int j = pl.t + b * P.T();
       if (j < nb) {
 #pragma unroll
         for (int r = 0; r < RR; ++r) {
@@ -292,11 +393,11 @@ __global__ void __launch_bounds__(1024) k_conv(FftArgs a, int kop) {
       }
     }
   });
-  run_passes<MAXE, true, STRIDED, Re>(v, pp, true, pl, sm, tw);
+  P.template run<true, true>(v, pl, sm, tw);
   const Re s = Re(a.scale);
-  radix_dispatch(pp.radix[0], [&](auto rc) {
+  P.template last<true>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
-    each_natural<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos, Cx<Re> val) {
+    each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos, Cx<Re> val) {
       if (pl.valid) Conv<S, Re>::st(out + pos * pl.ps, scale(val, s));
     });
   });
@@ -308,10 +409,12 @@ __global__ void __launch_bounds__(1024) k_conv(FftArgs a, int kop) {
 // z[m] = x[2m] + i x[2m+1] -> Z = FFT_n(z) ->
 // X[k] = (Z[k] + conj Z[n-k])/2 - i W_2n^k (Z[k] - conj Z[n-k])/2, k = 0..n
 // ---------------------------------------------------------------------------
-template <int MAXE, class S, class Re>
+template <class Plan, class S, class Re>
 __global__ void __launch_bounds__(1024) k_r2c_even(FftArgs a) {
   using SR = typename RealOf<S>::type;
-  const Place<false> pl(a);
+  const Plan P(a.pp);
+  constexpr int MAXE = Plan::MAXE;
+  const Place<false> pl(a, P.T());
   const PassPlan& pp = a.pp;
   Cx<Re>* sm = smem_base<Re>();
   const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
@@ -320,12 +423,12 @@ __global__ void __launch_bounds__(1024) k_r2c_even(FftArgs a) {
   const SR* inr = reinterpret_cast<const SR*>(in);
   S* out = reinterpret_cast<S*>(a.out) + pl.out0;
   Cx<Re> v[MAXE];
-  const int n = pp.n;
+  const int n = P.n();
   const int lo = a.sig_lo, hi = a.sig_hi;
   const bool full = lo <= 0 && hi >= 2 * n;
-  radix_dispatch(pp.radix[0], [&](auto rc) {
+  P.template first<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
-    gather<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos) {
+    gather<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos) {
       if (!pl.valid) return mk<Re>(Re(0), Re(0));
       if (full) return Conv<S, Re>::ld(in + pos);
       const int e = 2 * pos, o = 2 * pos + 1;
@@ -334,18 +437,17 @@ __global__ void __launch_bounds__(1024) k_r2c_even(FftArgs a) {
       return mk<Re>(xr, xi);
     });
   });
-  run_passes<MAXE, false, false, Re>(v, pp, false, pl, sm, tw);
-  const int RL = pp.radix[pp.npass - 1];
+  P.template run<false, false>(v, pl, sm, tw);
   __syncthreads();
-  radix_dispatch(RL, [&](auto rc) {
+  P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
-    each_natural<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos, Cx<Re> val) { sm[pl.sidx(pp, pos)] = val; });
+    each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos, Cx<Re> val) { sm[pl.sidx(pp, pos)] = val; });
   });
   __syncthreads();
   const Re half = Re(0.5);
-  radix_dispatch(RL, [&](auto rc) {
+  P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
-    each_natural<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int k, Cx<Re> zk) {
+    each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int k, Cx<Re> zk) {
       const int kc = k == 0 ? 0 : n - k;
       const Cx<Re> zc = conj(sm[pl.sidx(pp, kc)]);
       const Cx<Re> e = scale(zk + zc, half);
@@ -367,9 +469,11 @@ __global__ void __launch_bounds__(1024) k_r2c_even(FftArgs a) {
 // imaginary parts of X[0] and X[n] dropped (the real part of the full-length
 // inverse does not depend on them) -> z = IFFT_n(Z) -> x[2m] + i x[2m+1] = z[m]
 // ---------------------------------------------------------------------------
-template <int MAXE, class S, class Re>
+template <class Plan, class S, class Re>
 __global__ void __launch_bounds__(1024) k_c2r_even(FftArgs a) {
-  const Place<false> pl(a);
+  const Plan P(a.pp);
+  constexpr int MAXE = Plan::MAXE;
+  const Place<false> pl(a, P.T());
   const PassPlan& pp = a.pp;
   Cx<Re>* sm = smem_base<Re>();
   const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
@@ -377,29 +481,29 @@ __global__ void __launch_bounds__(1024) k_c2r_even(FftArgs a) {
   const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
   S* out = reinterpret_cast<S*>(a.out) + pl.out0;
   Cx<Re> v[MAXE];
-  const int n = pp.n;
-  for (int i = pl.t; i <= n; i += pp.T) {
+  const int n = P.n();
+  for (int i = pl.t; i <= n; i += P.T()) {
     Cx<Re> x = pl.valid ? Conv<S, Re>::ld(in + i) : mk<Re>(Re(0), Re(0));
     if (i == 0 || i == n) x.y = Re(0);
     sm[pl.sidx(pp, i)] = x;
   }
   __syncthreads();
-  radix_dispatch(pp.radix[0], [&](auto rc) {
+  P.template first<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
-    gather<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int k) {
+    gather<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int k) {
       const Cx<Re> xk = sm[pl.sidx(pp, k)];
       const Cx<Re> xc = conj(sm[pl.sidx(pp, n - k)]);
       const Cx<Re> s = xk + xc;
       const Cx<Re> d = xk - xc;
       const Cx<Re> wd = cmulc(d, ldg(&tw2[k]));  // d * W^{-k}
-      return mk<Re>(s.x - wd.y, s.y + wd.x);      // s + i*wd
+      return mk<Re>(s.x - wd.y, s.y + wd.x);     // s + i*wd
     });
   });
-  run_passes<MAXE, true, false, Re>(v, pp, false, pl, sm, tw);
+  P.template run<true, false>(v, pl, sm, tw);
   const Re s = Re(a.scale);
-  radix_dispatch(pp.radix[pp.npass - 1], [&](auto rc) {
+  P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
-    each_natural<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos, Cx<Re> val) {
+    each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos, Cx<Re> val) {
       if (pl.valid) Conv<S, Re>::st(out + pos, scale(val, s));
     });
   });
@@ -412,22 +516,23 @@ __global__ void __launch_bounds__(1024) k_c2r_even(FftArgs a) {
 // reference's own R2C I/O rules (vkdispatch/fft/global_memory_iterators.py:
 // 85-92, 214-226).  Row pitch N+1 reals = N/2+1 complex.
 // ---------------------------------------------------------------------------
-template <int MAXE, bool INV, class S, class Re>
+template <class Plan, bool INV, class S, class Re>
 __global__ void __launch_bounds__(1024) k_real_odd(FftArgs a) {
   using SR = typename RealOf<S>::type;
-  const Place<false> pl(a);
-  const PassPlan& pp = a.pp;
+  const Plan P(a.pp);
+  constexpr int MAXE = Plan::MAXE;
+  const Place<false> pl(a, P.T());
   Cx<Re>* sm = smem_base<Re>();
   const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
   const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
   S* out = reinterpret_cast<S*>(a.out) + pl.out0;
   Cx<Re> v[MAXE];
-  const int n = pp.n;
+  const int n = P.n();
   const int h = n / 2;
   const int lo = a.sig_lo, hi = a.sig_hi;
-  radix_dispatch(pp.radix[0], [&](auto rc) {
+  P.template first<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
-    gather<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos) {
+    gather<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos) {
       if (!pl.valid) return mk<Re>(Re(0), Re(0));
       if (!INV) {
         if (pos < lo || pos >= hi) return mk<Re>(Re(0), Re(0));
@@ -437,11 +542,11 @@ __global__ void __launch_bounds__(1024) k_real_odd(FftArgs a) {
       return conj(Conv<S, Re>::ld(in + (n - pos)));
     });
   });
-  run_passes<MAXE, INV, false, Re>(v, pp, false, pl, sm, tw);
+  P.template run<INV, false>(v, pl, sm, tw);
   const Re s = Re(a.scale);
-  radix_dispatch(pp.radix[pp.npass - 1], [&](auto rc) {
+  P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
-    each_natural<RR, MAXE, Re>(v, n / RR, pp.T, pl.t, [&](int pos, Cx<Re> val) {
+    each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos, Cx<Re> val) {
       if (!pl.valid) return;
       if (!INV) {
         if (pos <= h) Conv<S, Re>::st(out + pos, val);
@@ -465,5 +570,26 @@ __global__ void k_twiddle(Cx<Re>* tab, int count, int den) {
   sincospi(2.0 * double(k) / double(den), &s, &c);
   tab[k] = mk<Re>(Re(c), Re(-s));
 }
+
+// ---------------------------------------------------------------------------
+// compile-time plans for power-of-two lengths (radix 16 passes, then the
+// leftover power of two); threads per transform = n / 16
+// ---------------------------------------------------------------------------
+template <int N>
+struct Pow2;
+template <> struct Pow2<16> { using L = RList<16>; static constexpr int T = 1; };
+template <> struct Pow2<32> { using L = RList<16, 2>; static constexpr int T = 2; };
+template <> struct Pow2<64> { using L = RList<16, 4>; static constexpr int T = 4; };
+template <> struct Pow2<128> { using L = RList<16, 8>; static constexpr int T = 8; };
+template <> struct Pow2<256> { using L = RList<16, 16>; static constexpr int T = 16; };
+template <> struct Pow2<512> { using L = RList<16, 16, 2>; static constexpr int T = 32; };
+template <> struct Pow2<1024> { using L = RList<16, 16, 4>; static constexpr int T = 64; };
+template <> struct Pow2<2048> { using L = RList<16, 16, 8>; static constexpr int T = 128; };
+template <> struct Pow2<4096> { using L = RList<16, 16, 16>; static constexpr int T = 256; };
+template <> struct Pow2<8192> { using L = RList<16, 16, 16, 2>; static constexpr int T = 512; };
+template <> struct Pow2<16384> { using L = RList<16, 16, 16, 4>; static constexpr int T = 1024; };
+
+template <int N>
+using Pow2Plan = FixPlan<N, Pow2<N>::T, typename Pow2<N>::L>;
 
 }  // namespace vdx

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -164,6 +165,7 @@ struct vdx_plan {
   bool f64;
   int store;
   int N;  // axis length (real length for R2C/C2R)
+  bool fixed;  // compile-time specialised kernels (complex64, power-of-two n)
   FftArgs args;
   Launch launch;
   std::vector<int> radices;
@@ -351,6 +353,8 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
   }
   p->launch.block = dim3(T * M);
   p->launch.smem = smem;
+  p->fixed = st == ST_C64 && !f64 && has_fixed_c64(n) && p->op != OP_R2C_ODD && p->op != OP_C2R_ODD &&
+             T == n / 16 && std::getenv("VDX_NO_FIXED") == nullptr;
 
   void* tw = nullptr;
   int rc = get_table(p->dev, n, n, f64, &tw);
@@ -384,9 +388,10 @@ int vdx_fft_plan_describe(const vdx_plan* p, char* buf, size_t n) {
   static const char* ops[] = {"c2c_fwd", "c2c_inv", "conv", "r2c_even", "c2r_even", "r2c_odd", "c2r_odd"};
   std::snprintf(buf, n,
                 "{\"op\": \"%s\", \"N\": %d, \"n\": %d, \"radices\": \"%s\", \"threads_per_transform\": %d, "
-                "\"transforms_per_cta\": %d, \"strided\": %s, \"grid\": %u, \"block\": %u, \"smem\": %zu}",
+                "\"transforms_per_cta\": %d, \"strided\": %s, \"fixed\": %s, \"grid\": %u, \"block\": %u, "
+                "\"smem\": %zu}",
                 ops[p->op], p->N, p->args.pp.n, r.c_str(), p->args.pp.T, p->args.pp.M, p->strided ? "true" : "false",
-                p->launch.grid.x, p->launch.block.x, p->launch.smem);
+                p->fixed ? "true" : "false", p->launch.grid.x, p->launch.block.x, p->launch.smem);
   return VDX_OK;
 }
 
@@ -404,6 +409,11 @@ int vdx_fft_exec(const vdx_plan* p, const void* in, void* out, const void* kerne
   a.ker = kernel;
   Launch l = p->launch;
   l.stream = reinterpret_cast<cudaStream_t>(stream);
+  if (p->fixed) {
+    e = launch_fixed_c64_any(p->args.pp.n, a, l, p->op, p->strided, p->d.kernel_op);
+    if (e != cudaSuccess) return cuda_fail(e, "FFT launch");
+    return VDX_OK;
+  }
   switch (p->store) {
     case ST_C64: e = launch_fft<Cx<float>, float>(a, l, p->op, p->strided, p->d.kernel_op); break;
     case ST_C32: e = launch_fft<c32s, float>(a, l, p->op, p->strided, p->d.kernel_op); break;

@@ -42,6 +42,13 @@ cudaError_t launch_fft(const FftArgs& a, const Launch& l, int op, bool strided, 
 
 cudaError_t launch_twiddle(void* tab, int count, int den, bool f64, cudaStream_t s);
 
+// complex64 kernels specialised at compile time for power-of-two n in
+// [16, 16384] (radix-16 passes, n/16 threads per transform)
+template <int N>
+cudaError_t launch_fixed_c64(const FftArgs& a, const Launch& l, int op, bool strided, int kop);
+bool has_fixed_c64(int n);
+cudaError_t launch_fixed_c64_any(int n, const FftArgs& a, const Launch& l, int op, bool strided, int kop);
+
 // Opt a kernel into more than 48 KB of dynamic shared memory once.
 template <class K>
 inline cudaError_t prepare_smem(K kernel, size_t smem) {

@@ -13,6 +13,7 @@ from __future__ import annotations
 import ctypes
 import dataclasses
 import inspect
+import re
 from typing import List, Optional, Union
 
 import numpy as np
@@ -97,17 +98,49 @@ def _trace_map(func, in_types) -> int:
     raise NotImplementedError(f"map {func.__name__} ({r!r}) is not in the supported map menu")
 
 
+def _signature(func):
+    """Signature with string annotations (``from __future__ import
+    annotations``) evaluated in the function's module."""
+    try:
+        return inspect.signature(func, eval_str=True)
+    except (NameError, TypeError, SyntaxError, AttributeError):
+        return inspect.signature(func)
+
+
+def _named_dtype(name: str):
+    t = getattr(vc, name, None)
+    if isinstance(t, dt.dtype):
+        return t
+    t = getattr(dt, name, None)
+    return t if isinstance(t, dt.dtype) else None
+
+
+def _resolve_annotation(a):
+    """String annotations that could not be evaluated (they name objects
+    local to an enclosing function) resolve by dtype name:
+    'x.Buff[x.complex64]' -> Buffer[complex64], 'x.float32' -> float32."""
+    if not isinstance(a, str):
+        return a
+    m = re.fullmatch(r"\s*(?:[\w.]*\.)?(?:Buff|Buffer)\[\s*(?:[\w.]*\.)?(\w+)\s*\]\s*", a)
+    if m and _named_dtype(m.group(1)) is not None:
+        return vc.Buffer[_named_dtype(m.group(1))]
+    m = re.fullmatch(r"\s*(?:[\w.]*\.)?(\w+)\s*", a)
+    if m and _named_dtype(m.group(1)) is not None:
+        return _named_dtype(m.group(1))
+    raise ValueError(f"cannot resolve the annotation {a!r} to a buffer or element type")
+
+
 class MappingFunction:
     """The reference's vd.map object: a function plus its buffer types."""
 
     def __init__(self, func, return_type=None, input_types=None):
         self.func = func
-        sig = inspect.signature(func)
+        sig = _signature(func)
         if return_type is None and sig.return_annotation is not inspect.Parameter.empty:
-            return_type = sig.return_annotation
+            return_type = _resolve_annotation(sig.return_annotation)
         self.return_type = return_type
         if input_types is None:
-            input_types = [p.annotation for p in sig.parameters.values()]
+            input_types = [_resolve_annotation(p.annotation) for p in sig.parameters.values()]
         self.buffer_types = list(input_types)
 
     def input_dtypes(self) -> List[dt.dtype]:
@@ -193,12 +226,13 @@ class ReduceFunction:
 
 def reduce(identity, axes=None, group_size=None, mapping_function: MappingFunction = None):
     def decorator(func):
-        sig = inspect.signature(func)
+        sig = _signature(func)
         if sig.return_annotation is inspect.Parameter.empty:
             raise ValueError("Return type must be annotated")
+        ret = _resolve_annotation(sig.return_annotation)
         op = _trace_reduction(func)
         mf = mapping_function
-        if mf is not None and mf.return_type != sig.return_annotation:
+        if mf is not None and mf.return_type != ret:
             raise ValueError("Mapping function return type must match the return type of the reduction function")
         return ReduceFunction(op, group_size=group_size, axes=axes, mapping_function=mf)
 
