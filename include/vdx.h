@@ -150,6 +150,33 @@ int vdx_reduce_partial_count(int64_t n, int64_t* partial_count);
 int vdx_reduce(int op, int map, int in_type, const void* in, int64_t n, int64_t batch, void* out,
                void* workspace, void* stream);
 
+/*
+ * vdx_reduce without a workspace: the same two launches and results, with
+ * the stage-1 partials kept in a fixed device array inside libvdx.  This
+ * entry point has no counterpart in the reference.
+ *
+ * It is for callers that cannot call cudaMalloc on the path that reduces:
+ * host applications whose device memory is owned by their own pool
+ * allocator, and latency-critical loops that cannot afford cudaMalloc's
+ * implicit device-wide synchronisation.  The caller still passes `in` and
+ * `out`; nothing is allocated or freed by this call.
+ *
+ *   - The array holds VDX_REDUCE_NOALLOC_SCRATCH_BYTES (1 MiB) on every GPU
+ *     that loads libvdx, for the life of the process.  A request needing
+ *     more (vdx_reduce_partial_count(n) * batch * output element size bytes)
+ *     fails with VDX_ERR_UNSUPPORTED and launches nothing.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - Every call shares the array, which keeps the last call's partials.
+ *     Stage 1 writes every slot stage 2 reads, so nothing needs clearing, but
+ *     calls that overlap on the GPU (other streams, other host threads) race
+ *     on it: serialise them.
+ */
+#define VDX_REDUCE_NOALLOC_SCRATCH_BYTES 1048576
+int vdx_reduce_noalloc(int op, int map, int in_type, const void* in, int64_t n, int64_t batch, void* out,
+                       void* stream);
+
 #ifdef __cplusplus
 }
 #endif

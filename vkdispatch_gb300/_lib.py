@@ -39,7 +39,9 @@ EXPORTED = (
     "vdx_fft_exec",
     "vdx_reduce_partial_count",
     "vdx_reduce",
+    "vdx_reduce_noalloc",
 )
+VDX_REDUCE_NOALLOC_SCRATCH_BYTES = 1048576
 
 
 class FftDesc(ctypes.Structure):
@@ -89,6 +91,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.vdx_reduce_partial_count.argtypes = [i64, ctypes.POINTER(i64)]
     lib.vdx_reduce.restype = i32
     lib.vdx_reduce.argtypes = [i32, i32, i32, vp, i64, i64, vp, vp, vp]
+    lib.vdx_reduce_noalloc.restype = i32
+    lib.vdx_reduce_noalloc.argtypes = [i32, i32, i32, vp, i64, i64, vp, vp]
 
 
 def lib() -> ctypes.CDLL:

@@ -13,7 +13,10 @@
 
 #include <math_constants.h>
 
+#include <cstdio>
 #include <limits>
+#include <map>
+#include <mutex>
 
 namespace vdx {
 
@@ -190,4 +193,73 @@ cudaError_t launch_reduce(int op, int map, int in_type, const void* in, long lon
   }
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free reduction: the stage-1 partials live in a fixed device
+// array instead of a caller-provided workspace.  Every GPU that loads libvdx
+// holds VDX_REDUCE_NOALLOC_SCRATCH_BYTES of it until the process exits.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_reduce_scratch[VDX_REDUCE_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+std::mutex g_scratch_mu;
+std::map<int, void*> g_scratch_addr;  // device ordinal -> device address of g_reduce_scratch
+
+// Host code only sees a host-side stand-in under the name g_reduce_scratch;
+// its device address comes from cudaGetSymbolAddress, resolved once per
+// device with that device current (the caller's current device).
+cudaError_t scratch_for_current_device(void** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  auto it = g_scratch_addr.find(dev);
+  if (it != g_scratch_addr.end()) {
+    *out = it->second;
+    return cudaSuccess;
+  }
+  void* p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_reduce_scratch);
+  if (e != cudaSuccess) return e;
+  g_scratch_addr[dev] = p;
+  *out = p;
+  return cudaSuccess;
+}
+
+}  // namespace
+
 }  // namespace vdx
+
+extern "C" int vdx_reduce_noalloc(int op, int map, int in_type, const void* in, int64_t n, int64_t batch, void* out,
+                                  void* stream) {
+  using namespace vdx;
+  int rc = check_reduce_args(op, map, in_type, in, n, batch, out);
+  if (rc != VDX_OK) return rc;
+  int64_t parts = 0;
+  rc = vdx_reduce_partial_count(n, &parts);
+  if (rc != VDX_OK) return rc;
+  const long long need = (long long)parts * batch * reduce_out_bytes(in_type);
+  if (need > (long long)VDX_REDUCE_NOALLOC_SCRATCH_BYTES) {
+    char msg[256];
+    std::snprintf(msg, sizeof(msg),
+                  "vdx_reduce_noalloc: %lld rows of %lld elements need %lld bytes of partials, above the %d-byte "
+                  "static scratch; use vdx_reduce with a workspace",
+                  (long long)batch, (long long)n, need, (int)VDX_REDUCE_NOALLOC_SCRATCH_BYTES);
+    return set_error(VDX_ERR_UNSUPPORTED, msg);
+  }
+  void* scratch = nullptr;
+  cudaError_t e = scratch_for_current_device(&scratch);
+  if (e != cudaSuccess) {
+    char msg[256];
+    std::snprintf(msg, sizeof(msg), "vdx_reduce_noalloc: cudaGetSymbolAddress of the scratch array failed: %s",
+                  cudaGetErrorString(e));
+    return set_error(VDX_ERR_CUDA, msg);
+  }
+  e = launch_reduce(op, map, in_type, in, n, batch, out, scratch, (int)parts, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) {
+    char msg[256];
+    std::snprintf(msg, sizeof(msg), "vdx_reduce_noalloc launch: %s", cudaGetErrorString(e));
+    return set_error(VDX_ERR_CUDA, msg);
+  }
+  return VDX_OK;
+}

@@ -157,6 +157,33 @@ size_t store_bytes(int st) { return st == ST_C128 ? 16 : st == ST_C64 ? 8 : 4; }
 
 }  // namespace
 
+namespace vdx {
+
+int set_error(int code, const char* msg) { return fail(code, msg); }
+
+int reduce_out_bytes(int in_type) { return in_type == VDX_F64 ? 8 : 4; }
+
+int check_reduce_args(int op, int map, int in_type, const void* in, long long n, long long batch, const void* out) {
+  if (!in || !out) return fail(VDX_ERR_INVALID, "in and out must be non-NULL device pointers");
+  if (n < 1 || batch < 1) return fail(VDX_ERR_INVALID, "n and batch must be >= 1");
+  if (batch > 65535) return fail(VDX_ERR_UNSUPPORTED, "batch above 65535 rows");
+  if (op < VDX_RED_ADD || op > VDX_RED_XOR) return fail(VDX_ERR_INVALID, "unknown reduction op");
+  if (map < VDX_MAP_IDENTITY || map > VDX_MAP_SIN) return fail(VDX_ERR_INVALID, "unknown map");
+  const bool integer = in_type == VDX_I32 || in_type == VDX_U32;
+  if (!integer && in_type != VDX_F32 && in_type != VDX_F64 && in_type != VDX_C64)
+    return fail(VDX_ERR_INVALID, "in_type must be F32, F64, C64, I32 or U32");
+  if (op >= VDX_RED_AND && !integer) return fail(VDX_ERR_INVALID, "bitwise reductions need integer input");
+  if (op >= VDX_RED_AND && map != VDX_MAP_IDENTITY) return fail(VDX_ERR_INVALID, "bitwise reductions take no map");
+  if (in_type == VDX_C64 && (map == VDX_MAP_IDENTITY || map == VDX_MAP_SIN))
+    return fail(VDX_ERR_INVALID, "complex input needs a map to a real value (abs, square, real, imag)");
+  if (in_type != VDX_C64 && (map == VDX_MAP_REAL || map == VDX_MAP_IMAG))
+    return fail(VDX_ERR_INVALID, "real/imag maps need complex input");
+  if (integer && map == VDX_MAP_SIN) return fail(VDX_ERR_INVALID, "sin map needs floating-point input");
+  return VDX_OK;
+}
+
+}  // namespace vdx
+
 struct vdx_plan {
   vdx_fft_desc d;
   int dev;
@@ -435,21 +462,9 @@ int vdx_reduce_partial_count(int64_t n, int64_t* partial_count) {
 
 int vdx_reduce(int op, int map, int in_type, const void* in, int64_t n, int64_t batch, void* out, void* workspace,
                void* stream) {
-  if (!in || !out || !workspace) return fail(VDX_ERR_INVALID, "in, out and workspace must be non-NULL");
-  if (n < 1 || batch < 1) return fail(VDX_ERR_INVALID, "n and batch must be >= 1");
-  if (batch > 65535) return fail(VDX_ERR_UNSUPPORTED, "batch above 65535 rows");
-  if (op < VDX_RED_ADD || op > VDX_RED_XOR) return fail(VDX_ERR_INVALID, "unknown reduction op");
-  if (map < VDX_MAP_IDENTITY || map > VDX_MAP_SIN) return fail(VDX_ERR_INVALID, "unknown map");
-  const bool integer = in_type == VDX_I32 || in_type == VDX_U32;
-  if (!integer && in_type != VDX_F32 && in_type != VDX_F64 && in_type != VDX_C64)
-    return fail(VDX_ERR_INVALID, "in_type must be F32, F64, C64, I32 or U32");
-  if (op >= VDX_RED_AND && !integer) return fail(VDX_ERR_INVALID, "bitwise reductions need integer input");
-  if (op >= VDX_RED_AND && map != VDX_MAP_IDENTITY) return fail(VDX_ERR_INVALID, "bitwise reductions take no map");
-  if (in_type == VDX_C64 && (map == VDX_MAP_IDENTITY || map == VDX_MAP_SIN))
-    return fail(VDX_ERR_INVALID, "complex input needs a map to a real value (abs, square, real, imag)");
-  if (in_type != VDX_C64 && (map == VDX_MAP_REAL || map == VDX_MAP_IMAG))
-    return fail(VDX_ERR_INVALID, "real/imag maps need complex input");
-  if (integer && map == VDX_MAP_SIN) return fail(VDX_ERR_INVALID, "sin map needs floating-point input");
+  int rc = check_reduce_args(op, map, in_type, in, n, batch, out);
+  if (rc != VDX_OK) return rc;
+  if (!workspace) return fail(VDX_ERR_INVALID, "workspace must be a non-NULL device pointer");
   int64_t parts = 0;
   vdx_reduce_partial_count(n, &parts);
   cudaError_t e = launch_reduce(op, map, in_type, in, n, batch, out, workspace, (int)parts,

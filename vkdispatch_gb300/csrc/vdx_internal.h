@@ -64,6 +64,11 @@ inline cudaError_t enqueue(K kernel, const Launch& l, Args... args) {
   return cudaGetLastError();
 }
 
+// error reporting and argument checks shared by the C entry points
+int set_error(int code, const char* msg);
+int check_reduce_args(int op, int map, int in_type, const void* in, long long n, long long batch, const void* out);
+int reduce_out_bytes(int in_type);
+
 // reductions
 cudaError_t launch_reduce(int op, int map, int in_type, const void* in, long long n, long long batch, void* out,
                           void* partials, int nparts, cudaStream_t s);
