@@ -80,12 +80,15 @@ def _load_peaks():
 
 
 def _load_traffic(kernel_name):
-    p = ROOT / "profiles" / "traffic.json"
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "ncu_traffic.txt"
     if not p.exists():
         return None
-    d = json.loads(p.read_text())
-    v = d.get(kernel_name)
-    return None if v is None else float(v)
+    for line in p.read_text().splitlines():
+        f = line.split()
+        if len(f) == 2 and not line.startswith("#") and f[0] == kernel_name:
+            return float(f[1])
+    return None
 
 
 class ClockSampler:
