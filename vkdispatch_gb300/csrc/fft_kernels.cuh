@@ -60,35 +60,48 @@ template <bool STRIDED>
 struct Place {
   int t, m;
   bool valid;
-  long long in0, out0, ker0;  // element offset of point 0
-  long long ps;               // point stride in elements
-  __device__ __forceinline__ Place(const FftArgs& a, int T) {
+  bool tile_full;  // every transform slot of this CTA exists (uniform per CTA)
+  long long ps;    // point stride in elements
+  const FftArgs& a;
+  __device__ __forceinline__ Place(const FftArgs& args, int T) : a(args) {
     const int tid = threadIdx.x;
     if (STRIDED) {
       m = tid % a.pp.M;
       t = tid / a.pp.M;
-      const long long o = blockIdx.x / a.col_tiles;
-      const long long c = (long long)(blockIdx.x % a.col_tiles) * a.pp.M + m;
+      const long long c = col();
       valid = c < a.inner;
-      in0 = o * a.in_bs + c;
-      out0 = o * a.out_bs + c;
-      ker0 = o * a.ker_bs + c;
+      tile_full = (long long)(blockIdx.x % a.col_tiles + 1) * a.pp.M <= a.inner;
       ps = a.inner;
     } else {
       t = tid % T;
       m = tid / T;
-      const long long g = (long long)blockIdx.x * a.pp.M + m;
-      valid = g < a.ntrans;
-      in0 = g * a.in_bs;
-      out0 = g * a.out_bs;
-      ker0 = g * a.ker_bs;
+      valid = row() < a.ntrans;
+      tile_full = (long long)(blockIdx.x + 1) * a.pp.M <= a.ntrans;
       ps = 1;
     }
   }
-  // shared-memory slot of point i of this thread's transform
+  // transform coordinates, recomputed where needed so that 64-bit offsets do
+  // not stay live across the passes
+  __device__ __forceinline__ long long col() const { return (long long)(blockIdx.x % a.col_tiles) * a.pp.M + m; }
+  __device__ __forceinline__ long long row() const { return (long long)blockIdx.x * a.pp.M + m; }
+  __device__ __forceinline__ long long off(long long bs) const {
+    if (STRIDED) return (long long)(blockIdx.x / a.col_tiles) * bs + col();
+    return row() * bs;
+  }
+  __device__ __forceinline__ long long in0() const { return off(a.in_bs); }
+  __device__ __forceinline__ long long out0() const { return off(a.out_bs); }
+  __device__ __forceinline__ long long ker0() const { return off(a.ker_bs); }
+  // shared-memory slot of point i of this thread's transform; padded by one
+  // slot every 16 so the stride-R scatters of the passes do not bank-conflict
   __device__ __forceinline__ int sidx(const PassPlan& pp, int i) const {
     if (STRIDED) return i * pp.M + m;
     return m * pp.npad + i + (i >> 4);
+  }
+  // unpadded slot, for exchanges whose accesses are unit-stride in either
+  // direction (the mirrored k / n-k accesses of the real transforms)
+  __device__ __forceinline__ int sidx_plain(const PassPlan& pp, int i) const {
+    if (STRIDED) return i * pp.M + m;
+    return m * pp.npad + i;
   }
 };
 
@@ -251,6 +264,7 @@ struct RRev<RList<>, RList<Os...>> {
 template <int MAXE_>
 struct DynPlan {
   static constexpr int MAXE = MAXE_;
+  __device__ __forceinline__ void assume_t(int) const {}
   const PassPlan& pp;
   __device__ __forceinline__ explicit DynPlan(const PassPlan& p) : pp(p) {}
   __device__ __forceinline__ int n() const { return pp.n; }
@@ -290,9 +304,12 @@ __device__ __forceinline__ void chain_list(RList<Rs...>, Cx<Re>* v, const PassPl
   chain<N, T, MAXE, INV, Re, STRIDED, 1, Rs...>(v, pp, pl, sm, tw);
 }
 
-template <int N_, int T_, class L>
+template <int N_, int T_, class L, int MAXE_ = 16>
 struct FixPlan {
-  static constexpr int MAXE = 16;
+  static constexpr int MAXE = MAXE_;
+  // the thread's index inside its transform is below T (lets the compiler
+  // drop the j < n/R guards of exact plans)
+  __device__ __forceinline__ void assume_t(int t) const { __builtin_assume(t >= 0 && t < T_); }
   const PassPlan& pp;
   __device__ __forceinline__ explicit FixPlan(const PassPlan& p) : pp(p) {}
   __device__ __forceinline__ static constexpr int n() { return N_; }
@@ -318,6 +335,47 @@ __device__ __forceinline__ Cx<Re>* smem_base() {
   return reinterpret_cast<Cx<Re>*>(vdx_smem_raw);
 }
 
+// First-pass gather of a complex input (signal-range masked).  CTAs whose
+// slots all exist and whose range is the whole axis take the unpredicated
+// path.
+template <class Plan, class S, class Re, bool STRIDED>
+__device__ __forceinline__ void gather_input(const Plan& P, const Place<STRIDED>& pl, const FftArgs& a, Cx<Re>* v,
+                                             const S* in) {
+  constexpr int MAXE = Plan::MAXE;
+  const int n = P.n();
+  const int lo = a.sig_lo, hi = a.sig_hi;
+  if (pl.tile_full && lo <= 0 && hi >= n) {
+    P.template first<false>([&](auto rc) {
+      constexpr int RR = decltype(rc)::value;
+      gather<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos) { return Conv<S, Re>::ld(in + pos * pl.ps); });
+    });
+  } else {
+    P.template first<false>([&](auto rc) {
+      constexpr int RR = decltype(rc)::value;
+      gather<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos) {
+        if (!pl.valid || pos < lo || pos >= hi) return mk<Re>(Re(0), Re(0));
+        return Conv<S, Re>::ld(in + pos * pl.ps);
+      });
+    });
+  }
+}
+
+// Natural-order store of the last executed pass, scaled.
+template <class Plan, bool REV, class S, class Re, bool STRIDED>
+__device__ __forceinline__ void store_output(const Plan& P, const Place<STRIDED>& pl, const FftArgs& a, Cx<Re>* v) {
+  constexpr int MAXE = Plan::MAXE;
+  S* out = reinterpret_cast<S*>(a.out) + pl.out0();
+  const int n = P.n();
+  const Re s = Re(a.scale);
+  const bool all = pl.tile_full;
+  P.template last<REV>([&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos, Cx<Re> val) {
+      if (all || pl.valid) Conv<S, Re>::st(out + pos * pl.ps, scale(val, s));
+    });
+  });
+}
+
 // ---------------------------------------------------------------------------
 // complex-to-complex
 // ---------------------------------------------------------------------------
@@ -328,26 +386,12 @@ __global__ void __launch_bounds__(1024) k_c2c(FftArgs a) {
   const Place<STRIDED> pl(a, P.T());
   Cx<Re>* sm = smem_base<Re>();
   const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
-  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
-  S* out = reinterpret_cast<S*>(a.out) + pl.out0;
+  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0();
   Cx<Re> v[MAXE];
-  const int n = P.n();
-  const int lo = a.sig_lo, hi = a.sig_hi;
-  P.template first<false>([&](auto rc) {
-    constexpr int RR = decltype(rc)::value;
-    gather<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos) {
-      if (!pl.valid || pos < lo || pos >= hi) return mk<Re>(Re(0), Re(0));
-      return Conv<S, Re>::ld(in + pos * pl.ps);
-    });
-  });
+  P.assume_t(pl.t);
+  gather_input<Plan, S, Re>(P, pl, a, v, in);
   P.template run<INV, false>(v, pl, sm, tw);
-  const Re s = Re(a.scale);
-  P.template last<false>([&](auto rc) {
-    constexpr int RR = decltype(rc)::value;
-    each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos, Cx<Re> val) {
-      if (pl.valid) Conv<S, Re>::st(out + pos * pl.ps, scale(val, s));
-    });
-  });
+  store_output<Plan, false, S, Re>(P, pl, a, v);
 }
 
 // ---------------------------------------------------------------------------
@@ -355,27 +399,21 @@ __global__ void __launch_bounds__(1024) k_c2c(FftArgs a) {
 // kop: 0 = multiply by conj(kernel) (reference default,
 // vkdispatch/fft/shader_factories.py:136-145), 1 = multiply by kernel.
 // ---------------------------------------------------------------------------
-template <class Plan, bool STRIDED, class S, class K, class Re>
-__global__ void __launch_bounds__(1024) k_conv(FftArgs a, int kop) {
+template <class Plan, bool STRIDED, class S, class K, class Re, int KOP>
+__global__ void __launch_bounds__(1024) k_conv(FftArgs a) {
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
   const Place<STRIDED> pl(a, P.T());
   Cx<Re>* sm = smem_base<Re>();
   const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
-  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
-  S* out = reinterpret_cast<S*>(a.out) + pl.out0;
-  const K* ker = reinterpret_cast<const K*>(a.ker) + pl.ker0;
+  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0();
   Cx<Re> v[MAXE];
+  P.assume_t(pl.t);
   const int n = P.n();
-  const int lo = a.sig_lo, hi = a.sig_hi;
-  P.template first<false>([&](auto rc) {
-    constexpr int RR = decltype(rc)::value;
-    gather<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos) {
-      if (!pl.valid || pos < lo || pos >= hi) return mk<Re>(Re(0), Re(0));
-      return Conv<S, Re>::ld(in + pos * pl.ps);
-    });
-  });
+  gather_input<Plan, S, Re>(P, pl, a, v, in);
+  const bool kvalid = pl.tile_full || pl.valid;
   P.template run<false, false>(v, pl, sm, tw);
+  const K* ker = reinterpret_cast<const K*>(a.ker) + pl.ker0();
   P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
     constexpr int B = MAXE / RR;
@@ -387,20 +425,14 @@ __global__ void __launch_bounds__(1024) k_conv(FftArgs a, int kop) {
 #pragma unroll
         for (int r = 0; r < RR; ++r) {
           const int pos = j + r * nb;
-          Cx<Re> kv = pl.valid ? Conv<K, Re>::ld(ker + pos * pl.ps) : mk<Re>(Re(0), Re(0));
-          v[b * RR + r] = kop == 0 ? cmulc(v[b * RR + r], kv) : cmul(v[b * RR + r], kv);
+          Cx<Re> kv = kvalid ? Conv<K, Re>::ld(ker + pos * pl.ps) : mk<Re>(Re(0), Re(0));
+          v[b * RR + r] = KOP == 0 ? cmulc(v[b * RR + r], kv) : cmul(v[b * RR + r], kv);
         }
       }
     }
   });
   P.template run<true, true>(v, pl, sm, tw);
-  const Re s = Re(a.scale);
-  P.template last<true>([&](auto rc) {
-    constexpr int RR = decltype(rc)::value;
-    each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos, Cx<Re> val) {
-      if (pl.valid) Conv<S, Re>::st(out + pos * pl.ps, scale(val, s));
-    });
-  });
+  store_output<Plan, true, S, Re>(P, pl, a, v);
 }
 
 // ---------------------------------------------------------------------------
@@ -419,18 +451,22 @@ __global__ void __launch_bounds__(1024) k_r2c_even(FftArgs a) {
   Cx<Re>* sm = smem_base<Re>();
   const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
   const Cx<Re>* tw2 = reinterpret_cast<const Cx<Re>*>(a.tw2);
-  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
+  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0();
   const SR* inr = reinterpret_cast<const SR*>(in);
-  S* out = reinterpret_cast<S*>(a.out) + pl.out0;
+  S* out = reinterpret_cast<S*>(a.out) + pl.out0();
   Cx<Re> v[MAXE];
+  P.assume_t(pl.t);
   const int n = P.n();
   const int lo = a.sig_lo, hi = a.sig_hi;
-  const bool full = lo <= 0 && hi >= 2 * n;
+  const bool full = lo <= 0 && hi >= 2 * n && pl.tile_full;
   P.template first<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
+    if (full) {
+      gather<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos) { return Conv<S, Re>::ld(in + pos); });
+      return;
+    }
     gather<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos) {
       if (!pl.valid) return mk<Re>(Re(0), Re(0));
-      if (full) return Conv<S, Re>::ld(in + pos);
       const int e = 2 * pos, o = 2 * pos + 1;
       Re xr = (e >= lo && e < hi) ? ld_real<Re>(inr + e) : Re(0);
       Re xi = (o >= lo && o < hi) ? ld_real<Re>(inr + o) : Re(0);
@@ -441,24 +477,26 @@ __global__ void __launch_bounds__(1024) k_r2c_even(FftArgs a) {
   __syncthreads();
   P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
-    each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos, Cx<Re> val) { sm[pl.sidx(pp, pos)] = val; });
+    each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t,
+                               [&](int pos, Cx<Re> val) { sm[pl.sidx_plain(pp, pos)] = val; });
   });
   __syncthreads();
   const Re half = Re(0.5);
+  const bool wr = pl.tile_full || pl.valid;
   P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
     each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int k, Cx<Re> zk) {
       const int kc = k == 0 ? 0 : n - k;
-      const Cx<Re> zc = conj(sm[pl.sidx(pp, kc)]);
+      const Cx<Re> zc = conj(sm[pl.sidx_plain(pp, kc)]);
       const Cx<Re> e = scale(zk + zc, half);
       const Cx<Re> d = scale(zk - zc, half);
       const Cx<Re> o = mk<Re>(d.y, -d.x);  // d / i
       const Cx<Re> x = e + cmul(ldg(&tw2[k]), o);
-      if (pl.valid) Conv<S, Re>::st(out + k, x);
+      if (wr) Conv<S, Re>::st(out + k, x);
     });
   });
   if (pl.t == 0 && pl.valid) {
-    const Cx<Re> z0 = sm[pl.sidx(pp, 0)];
+    const Cx<Re> z0 = sm[pl.sidx_plain(pp, 0)];
     Conv<S, Re>::st(out + n, mk<Re>(z0.x - z0.y, Re(0)));
   }
 }
@@ -478,21 +516,38 @@ __global__ void __launch_bounds__(1024) k_c2r_even(FftArgs a) {
   Cx<Re>* sm = smem_base<Re>();
   const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
   const Cx<Re>* tw2 = reinterpret_cast<const Cx<Re>*>(a.tw2);
-  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
-  S* out = reinterpret_cast<S*>(a.out) + pl.out0;
+  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0();
   Cx<Re> v[MAXE];
+  P.assume_t(pl.t);
   const int n = P.n();
-  for (int i = pl.t; i <= n; i += P.T()) {
-    Cx<Re> x = pl.valid ? Conv<S, Re>::ld(in + i) : mk<Re>(Re(0), Re(0));
-    if (i == 0 || i == n) x.y = Re(0);
-    sm[pl.sidx(pp, i)] = x;
+  // X[0..n-1] through registers with every load in flight before the first
+  // shared-memory store (n <= T * MAXE for every plan); X[n] by thread 0
+  const bool ld_ok = pl.tile_full || pl.valid;
+#pragma unroll
+  for (int u = 0; u < MAXE; ++u) {
+    const int i = pl.t + u * P.T();
+    if (i < n) v[u] = ld_ok ? Conv<S, Re>::ld(in + i) : mk<Re>(Re(0), Re(0));
+  }
+#pragma unroll
+  for (int u = 0; u < MAXE; ++u) {
+    const int i = pl.t + u * P.T();
+    if (i < n) {
+      Cx<Re> x = v[u];
+      if (i == 0) x.y = Re(0);
+      sm[pl.sidx_plain(pp, i)] = x;
+    }
+  }
+  if (pl.t == 0) {
+    Cx<Re> x = ld_ok ? Conv<S, Re>::ld(in + n) : mk<Re>(Re(0), Re(0));
+    x.y = Re(0);
+    sm[pl.sidx_plain(pp, n)] = x;
   }
   __syncthreads();
   P.template first<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
     gather<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int k) {
-      const Cx<Re> xk = sm[pl.sidx(pp, k)];
-      const Cx<Re> xc = conj(sm[pl.sidx(pp, n - k)]);
+      const Cx<Re> xk = sm[pl.sidx_plain(pp, k)];
+      const Cx<Re> xc = conj(sm[pl.sidx_plain(pp, n - k)]);
       const Cx<Re> s = xk + xc;
       const Cx<Re> d = xk - xc;
       const Cx<Re> wd = cmulc(d, ldg(&tw2[k]));  // d * W^{-k}
@@ -500,13 +555,7 @@ __global__ void __launch_bounds__(1024) k_c2r_even(FftArgs a) {
     });
   });
   P.template run<true, false>(v, pl, sm, tw);
-  const Re s = Re(a.scale);
-  P.template last<false>([&](auto rc) {
-    constexpr int RR = decltype(rc)::value;
-    each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos, Cx<Re> val) {
-      if (pl.valid) Conv<S, Re>::st(out + pos, scale(val, s));
-    });
-  });
+  store_output<Plan, false, S, Re>(P, pl, a, v);
 }
 
 // ---------------------------------------------------------------------------
@@ -524,8 +573,8 @@ __global__ void __launch_bounds__(1024) k_real_odd(FftArgs a) {
   const Place<false> pl(a, P.T());
   Cx<Re>* sm = smem_base<Re>();
   const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
-  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0;
-  S* out = reinterpret_cast<S*>(a.out) + pl.out0;
+  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0();
+  S* out = reinterpret_cast<S*>(a.out) + pl.out0();
   Cx<Re> v[MAXE];
   const int n = P.n();
   const int h = n / 2;
@@ -591,5 +640,6 @@ template <> struct Pow2<16384> { using L = RList<16, 16, 16, 4>; static constexp
 
 template <int N>
 using Pow2Plan = FixPlan<N, Pow2<N>::T, typename Pow2<N>::L>;
+
 
 }  // namespace vdx

@@ -16,8 +16,12 @@ cudaError_t launch_with_plan(const FftArgs& a, const Launch& l, int op, bool str
       if (strided) return enqueue(k_c2c<Plan, true, true, S, Re>, l, a);
       return enqueue(k_c2c<Plan, true, false, S, Re>, l, a);
     case OP_CONV:
-      if (strided) return enqueue(k_conv<Plan, true, S, S, Re>, l, a, kop);
-      return enqueue(k_conv<Plan, false, S, S, Re>, l, a, kop);
+      if (kop == 0) {
+        if (strided) return enqueue(k_conv<Plan, true, S, S, Re, 0>, l, a);
+        return enqueue(k_conv<Plan, false, S, S, Re, 0>, l, a);
+      }
+      if (strided) return enqueue(k_conv<Plan, true, S, S, Re, 1>, l, a);
+      return enqueue(k_conv<Plan, false, S, S, Re, 1>, l, a);
     case OP_R2C_EVEN:
       return enqueue(k_r2c_even<Plan, S, Re>, l, a);
     case OP_C2R_EVEN:

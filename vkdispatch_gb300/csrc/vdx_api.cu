@@ -304,13 +304,17 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
   int M = 1;
   size_t smem = 0;
   if (strided) {
-    M = (int)std::min<long long>(16, inner);
+    int mcols = 8;
+    if (const char* e = std::getenv("VDX_STRIDED_COLUMNS")) mcols = std::max(1, std::min(32, std::atoi(e)));
+    M = (int)std::min<long long>(mcols, inner);
     M = std::max(1, std::min(M, 1024 / T));
     while (M > 1 && need_smem && size_t(n) * M * cbytes > size_t(smem_optin)) M /= 2;
     smem = need_smem ? size_t(n) * M * cbytes : 0;
   } else {
     const long long ntrans = outer;
-    M = std::max(1, 256 / T);
+    int cta_threads = 128;
+    if (const char* e = std::getenv("VDX_CTA_THREADS")) cta_threads = std::max(32, std::min(1024, std::atoi(e)));
+    M = std::max(1, cta_threads / T);
     M = (int)std::min<long long>(M, ntrans);
     M = std::max(1, std::min(M, 1024 / T));
     while (M > 1 && need_smem && size_t(npad) * M * cbytes > size_t(smem_optin) / 2) M /= 2;
@@ -320,7 +324,6 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
     delete p;
     return fail(VDX_ERR_UNSUPPORTED, "FFT length " + std::to_string(n) + " does not fit in shared memory");
   }
-
   FftArgs& a = p->args;
   std::memset(&a, 0, sizeof(a));
   a.pp.n = n;
@@ -380,8 +383,8 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
   }
   p->launch.block = dim3(T * M);
   p->launch.smem = smem;
-  p->fixed = st == ST_C64 && !f64 && has_fixed_c64(n) && p->op != OP_R2C_ODD && p->op != OP_C2R_ODD &&
-             T == n / 16 && std::getenv("VDX_NO_FIXED") == nullptr;
+  p->fixed = st == ST_C64 && !f64 && has_fixed_c64(n) && p->op != OP_R2C_ODD &&
+             p->op != OP_C2R_ODD && T == n / 16 && std::getenv("VDX_NO_FIXED") == nullptr;
 
   void* tw = nullptr;
   int rc = get_table(p->dev, n, n, f64, &tw);
