@@ -61,7 +61,7 @@ typedef struct vdx_fft_desc {
   int32_t axis;       /* transformed axis (R2C/C2R: must be ndim-1) */
   int32_t kind;       /* VDX_KIND_* */
   int32_t inverse;    /* C2C: 0 forward (exp(-2 pi i nk/N)), 1 inverse */
-  int32_t normalize;  /* inverse / C2R / CONV: scale by 1/N */
+  int32_t normalize;  /* C2C / C2R / CONV: scale the output by 1/N (R2C: ignored) */
   int32_t io_type;    /* VDX_C64, VDX_C32, VDX_C128 or VDX_BF16X2 */
   int32_t compute_type; /* VDX_C64 (fp32 butterflies) or VDX_C128 (fp64) */
   int64_t signal_lo;  /* input_signal_range: points outside [lo, hi) read as 0; */
@@ -112,6 +112,38 @@ int vdx_fft_plan_describe(const vdx_plan* plan, char* buf, size_t n);
  *            when kernel_broadcast = 1).
  */
 int vdx_fft_exec(const vdx_plan* plan, const void* in, void* out, const void* kernel, void* stream);
+
+/*
+ * Fused element-wise operations for the adjoint (autograd) pipelines of FFT
+ * convolutions; complex64 plans only, at most one operation per launch.  The
+ * weight and auxiliary arrays have the buffer's shape and are indexed like
+ * it.  No counterpart in the reference, whose gradients do not exist; these
+ * serve the differentiable convolution (vkdispatch_gb300/autograd.py).
+ *   in_weight   (C2C)  : each input point is multiplied by
+ *                        in_weight[i] * in_weight_scale (* *in_weight_scale_ptr
+ *                        when that device pointer is set) as it is loaded
+ *   spec_out    (CONV) : receives the forward spectrum S of every transform,
+ *                        or, with spec_aux set, spec_aux * conj(S) * spec_scale
+ *   loss_weight (C2C)  : each CTA writes sum(loss_weight[i] * |out[i]|^2) over
+ *                        its outputs to loss_partials[cta] (vdx_fft_plan_ctas
+ *                        entries); fold them with vdx_reduce for the total
+ */
+typedef struct vdx_exec_ops {
+  const float* in_weight;
+  const float* in_weight_scale_ptr;
+  float in_weight_scale;
+  float spec_scale;
+  void* spec_out;
+  const void* spec_aux;
+  const float* loss_weight;
+  float* loss_partials;
+} vdx_exec_ops;
+
+int vdx_fft_exec_ops(const vdx_plan* plan, const void* in, void* out, const void* kernel, const vdx_exec_ops* ops,
+                     void* stream);
+
+/* Number of CTAs one vdx_fft_exec of this plan launches. */
+int vdx_fft_plan_ctas(const vdx_plan* plan, int64_t* ctas);
 
 /* reduction operations (vkdispatch/reduce/operations.py:17-66) */
 #define VDX_RED_ADD 0

@@ -40,6 +40,8 @@ EXPORTED = (
     "vdx_reduce_partial_count",
     "vdx_reduce",
     "vdx_reduce_noalloc",
+    "vdx_fft_exec_ops",
+    "vdx_fft_plan_ctas",
 )
 VDX_REDUCE_NOALLOC_SCRATCH_BYTES = 1048576
 
@@ -60,6 +62,19 @@ class FftDesc(ctypes.Structure):
         ("kernel_type", ctypes.c_int32),
         ("kernel_broadcast", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
+    ]
+
+
+class ExecOps(ctypes.Structure):
+    _fields_ = [
+        ("in_weight", ctypes.c_void_p),
+        ("in_weight_scale_ptr", ctypes.c_void_p),
+        ("in_weight_scale", ctypes.c_float),
+        ("spec_scale", ctypes.c_float),
+        ("spec_out", ctypes.c_void_p),
+        ("spec_aux", ctypes.c_void_p),
+        ("loss_weight", ctypes.c_void_p),
+        ("loss_partials", ctypes.c_void_p),
     ]
 
 
@@ -91,6 +106,10 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.vdx_reduce_partial_count.argtypes = [i64, ctypes.POINTER(i64)]
     lib.vdx_reduce.restype = i32
     lib.vdx_reduce.argtypes = [i32, i32, i32, vp, i64, i64, vp, vp, vp]
+    lib.vdx_fft_exec_ops.restype = i32
+    lib.vdx_fft_exec_ops.argtypes = [vp, vp, vp, vp, ctypes.POINTER(ExecOps), vp]
+    lib.vdx_fft_plan_ctas.restype = i32
+    lib.vdx_fft_plan_ctas.argtypes = [vp, ctypes.POINTER(i64)]
     lib.vdx_reduce_noalloc.restype = i32
     lib.vdx_reduce_noalloc.argtypes = [i32, i32, i32, vp, i64, i64, vp, vp]
 

@@ -7,19 +7,20 @@ bool has_fixed_c64(int n) {
   return n >= 16 && n <= 16384 && (n & (n - 1)) == 0;
 }
 
-cudaError_t launch_fixed_c64_any(int n, const FftArgs& a, const Launch& l, int op, bool strided, int kop) {
+cudaError_t launch_fixed_c64_any(int n, const FftArgs& a, const Launch& l, int op, bool strided, int kop,
+                                 int variant) {
   switch (n) {
-    case 16: return launch_fixed_c64<16>(a, l, op, strided, kop);
-    case 32: return launch_fixed_c64<32>(a, l, op, strided, kop);
-    case 64: return launch_fixed_c64<64>(a, l, op, strided, kop);
-    case 128: return launch_fixed_c64<128>(a, l, op, strided, kop);
-    case 256: return launch_fixed_c64<256>(a, l, op, strided, kop);
-    case 512: return launch_fixed_c64<512>(a, l, op, strided, kop);
-    case 1024: return launch_fixed_c64<1024>(a, l, op, strided, kop);
-    case 2048: return launch_fixed_c64<2048>(a, l, op, strided, kop);
-    case 4096: return launch_fixed_c64<4096>(a, l, op, strided, kop);
-    case 8192: return launch_fixed_c64<8192>(a, l, op, strided, kop);
-    case 16384: return launch_fixed_c64<16384>(a, l, op, strided, kop);
+    case 16: return launch_fixed_c64<16>(a, l, op, strided, kop, variant);
+    case 32: return launch_fixed_c64<32>(a, l, op, strided, kop, variant);
+    case 64: return launch_fixed_c64<64>(a, l, op, strided, kop, variant);
+    case 128: return launch_fixed_c64<128>(a, l, op, strided, kop, variant);
+    case 256: return launch_fixed_c64<256>(a, l, op, strided, kop, variant);
+    case 512: return launch_fixed_c64<512>(a, l, op, strided, kop, variant);
+    case 1024: return launch_fixed_c64<1024>(a, l, op, strided, kop, variant);
+    case 2048: return launch_fixed_c64<2048>(a, l, op, strided, kop, variant);
+    case 4096: return launch_fixed_c64<4096>(a, l, op, strided, kop, variant);
+    case 8192: return launch_fixed_c64<8192>(a, l, op, strided, kop, variant);
+    case 16384: return launch_fixed_c64<16384>(a, l, op, strided, kop, variant);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -51,6 +51,15 @@ struct FftArgs {
   int sig_lo, sig_hi;     // input positions outside [lo, hi) read as zero
   double scale;           // applied at the final store
   int nreal;              // real transforms: logical real length N
+  // fused element-wise operations (complex64 kernels; see vdx_exec_ops)
+  const float* in_weight;  // C2C: input point *= in_weight[element] * in_weight_scale on load
+  const float* in_weight_scale_ptr;  // optional device scalar multiplied into in_weight_scale
+  float in_weight_scale;
+  float spec_scale;        // CONV: spec_out = spec_aux * conj(S) * spec_scale (mode 2)
+  void* spec_out;          // CONV: receives the forward spectrum S (mode 1) or the product (mode 2)
+  const void* spec_aux;
+  const float* loss_weight;  // C2C: per-CTA partial of sum(loss_weight * |out|^2)
+  float* loss_partials;
 };
 
 // ---------------------------------------------------------------------------
@@ -379,7 +388,10 @@ __device__ __forceinline__ void store_output(const Plan& P, const Place<STRIDED>
 // ---------------------------------------------------------------------------
 // complex-to-complex
 // ---------------------------------------------------------------------------
-template <class Plan, bool INV, bool STRIDED, class S, class Re>
+// IW: multiply each input point by in_weight[element] * in_weight_scale as it
+// is loaded (the 2 w y of a weighted |y|^2 loss's gradient).
+// LOSS: write one partial of sum(loss_weight[element] * |output|^2) per CTA.
+template <class Plan, bool INV, bool STRIDED, class S, class Re, int IW = 0, int LOSS = 0>
 __global__ void __launch_bounds__(1024) k_c2c(FftArgs a) {
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
@@ -389,9 +401,60 @@ __global__ void __launch_bounds__(1024) k_c2c(FftArgs a) {
   const S* in = reinterpret_cast<const S*>(a.in) + pl.in0();
   Cx<Re> v[MAXE];
   P.assume_t(pl.t);
+  const int n = P.n();
   gather_input<Plan, S, Re>(P, pl, a, v, in);
+  if constexpr (IW) {
+    const float* w = a.in_weight + pl.in0();
+    const Re f = Re(a.in_weight_scale) * (a.in_weight_scale_ptr ? Re(__ldg(a.in_weight_scale_ptr)) : Re(1));
+    const bool ok = pl.tile_full || pl.valid;
+    P.template first<false>([&](auto rc) {
+      constexpr int RR = decltype(rc)::value;
+      constexpr int B = MAXE / RR;
+      const int nb = n / RR;
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        const int j = pl.t + b * P.T();
+        if (j < nb) {
+#pragma unroll
+          for (int r = 0; r < RR; ++r) {
+            const Re wv = ok ? Re(__ldg(w + (j + r * nb) * pl.ps)) * f : Re(0);
+            v[b * RR + r] = scale(v[b * RR + r], wv);
+          }
+        }
+      }
+    });
+  }
   P.template run<INV, false>(v, pl, sm, tw);
   store_output<Plan, false, S, Re>(P, pl, a, v);
+  if constexpr (LOSS) {
+    const float* lw = a.loss_weight + pl.out0();
+    const Re s = Re(a.scale);
+    const bool ok = pl.tile_full || pl.valid;
+    float acc = 0.f;
+    P.template last<false>([&](auto rc) {
+      constexpr int RR = decltype(rc)::value;
+      each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos, Cx<Re> val) {
+        if (ok) {
+          const Cx<Re> y = scale(val, s);
+          acc += __ldg(lw + pos * pl.ps) * float(y.x * y.x + y.y * y.y);
+        }
+      });
+    });
+    // block sum in a fixed order through shared memory (any CTA size; the
+    // plan reserves blockDim floats of dynamic shared memory)
+    float* red = reinterpret_cast<float*>(sm);
+    const int nt = blockDim.x, tid = threadIdx.x;
+    __syncthreads();
+    red[tid] = acc;
+    __syncthreads();
+    int span = 1;
+    while (span < nt) span <<= 1;
+    for (int h = span >> 1; h > 0; h >>= 1) {
+      if (tid < h && tid + h < nt) red[tid] += red[tid + h];
+      __syncthreads();
+    }
+    if (tid == 0) a.loss_partials[blockIdx.x] = red[0];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -399,7 +462,10 @@ __global__ void __launch_bounds__(1024) k_c2c(FftArgs a) {
 // kop: 0 = multiply by conj(kernel) (reference default,
 // vkdispatch/fft/shader_factories.py:136-145), 1 = multiply by kernel.
 // ---------------------------------------------------------------------------
-template <class Plan, bool STRIDED, class S, class K, class Re, int KOP>
+// SPEC 1: also write the forward spectrum S to spec_out (kept for a backward
+// pass).  SPEC 2: write spec_aux * conj(S) * spec_scale to spec_out instead
+// (the kernel-spectrum gradient X conj(G) / N of an FFT convolution).
+template <class Plan, bool STRIDED, class S, class K, class Re, int KOP, int SPEC = 0>
 __global__ void __launch_bounds__(1024) k_conv(FftArgs a) {
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
@@ -413,6 +479,23 @@ __global__ void __launch_bounds__(1024) k_conv(FftArgs a) {
   gather_input<Plan, S, Re>(P, pl, a, v, in);
   const bool kvalid = pl.tile_full || pl.valid;
   P.template run<false, false>(v, pl, sm, tw);
+  if constexpr (SPEC != 0) {
+    S* so = reinterpret_cast<S*>(a.spec_out) + pl.out0();
+    const S* sa = reinterpret_cast<const S*>(a.spec_aux) + pl.out0();
+    const Re ss = Re(a.spec_scale);
+    P.template last<false>([&](auto rc) {
+      constexpr int RR = decltype(rc)::value;
+      each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int pos, Cx<Re> val) {
+        if (!kvalid) return;
+        if (SPEC == 1) {
+          Conv<S, Re>::st(so + pos * pl.ps, val);
+        } else {
+          const Cx<Re> x = Conv<S, Re>::ld(sa + pos * pl.ps);
+          Conv<S, Re>::st(so + pos * pl.ps, scale(cmulc(x, val), ss));
+        }
+      });
+    });
+  }
   const K* ker = reinterpret_cast<const K*>(a.ker) + pl.ker0();
   P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;

@@ -320,6 +320,9 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
     while (M > 1 && need_smem && size_t(npad) * M * cbytes > size_t(smem_optin) / 2) M /= 2;
     smem = need_smem ? size_t(npad) * M * cbytes : 0;
   }
+  // the fused loss epilogue of C2C launches reduces one float per thread
+  // through shared memory, so every C2C plan reserves at least that much
+  if (d.kind == VDX_KIND_C2C) smem = std::max(smem, size_t(T) * size_t(M) * sizeof(float));
   if (smem > size_t(smem_optin)) {
     delete p;
     return fail(VDX_ERR_UNSUPPORTED, "FFT length " + std::to_string(n) + " does not fit in shared memory");
@@ -340,7 +343,7 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
   switch (d.kind) {
     case VDX_KIND_C2C:
       p->op = d.inverse ? OP_C2C_INV : OP_C2C_FWD;
-      a.scale = (d.inverse && norm) ? 1.0 / N : 1.0;
+      a.scale = norm ? 1.0 / N : 1.0;
       break;
     case VDX_KIND_CONV:
       p->op = OP_CONV;
@@ -425,7 +428,10 @@ int vdx_fft_plan_describe(const vdx_plan* p, char* buf, size_t n) {
   return VDX_OK;
 }
 
-int vdx_fft_exec(const vdx_plan* p, const void* in, void* out, const void* kernel, void* stream) {
+namespace {
+
+int exec_plan(const vdx_plan* p, const void* in, void* out, const void* kernel, const vdx_exec_ops* ops,
+              void* stream) {
   if (!p) return fail(VDX_ERR_INVALID, "plan is NULL");
   if (!in || !out) return fail(VDX_ERR_INVALID, "in and out must be non-NULL device pointers");
   if (p->op == OP_CONV && !kernel) return fail(VDX_ERR_INVALID, "convolution needs a kernel spectrum");
@@ -437,21 +443,64 @@ int vdx_fft_exec(const vdx_plan* p, const void* in, void* out, const void* kerne
   a.in = in;
   a.out = out;
   a.ker = kernel;
+  int variant = 0;
+  if (ops) {
+    const int nops = (ops->in_weight != nullptr) + (ops->spec_out != nullptr) + (ops->loss_weight != nullptr);
+    if (nops > 1) return fail(VDX_ERR_INVALID, "at most one fused operation per launch");
+    if (nops == 1 && p->store != ST_C64) return fail(VDX_ERR_UNSUPPORTED, "fused operations need complex64 plans");
+    const bool c2c = p->op == OP_C2C_FWD || p->op == OP_C2C_INV;
+    if (ops->in_weight) {
+      if (!c2c) return fail(VDX_ERR_INVALID, "in_weight applies to C2C plans");
+      variant = 1;
+      a.in_weight = ops->in_weight;
+      a.in_weight_scale_ptr = ops->in_weight_scale_ptr;
+      a.in_weight_scale = ops->in_weight_scale;
+    } else if (ops->loss_weight) {
+      if (!c2c) return fail(VDX_ERR_INVALID, "loss_weight applies to C2C plans");
+      if (!ops->loss_partials) return fail(VDX_ERR_INVALID, "loss_weight needs loss_partials");
+      variant = 2;
+      a.loss_weight = ops->loss_weight;
+      a.loss_partials = ops->loss_partials;
+    } else if (ops->spec_out) {
+      if (p->op != OP_CONV) return fail(VDX_ERR_INVALID, "spec_out applies to convolution plans");
+      variant = ops->spec_aux ? 2 : 1;
+      a.spec_out = ops->spec_out;
+      a.spec_aux = ops->spec_aux;
+      a.spec_scale = ops->spec_scale;
+    }
+  }
   Launch l = p->launch;
   l.stream = reinterpret_cast<cudaStream_t>(stream);
   if (p->fixed) {
-    e = launch_fixed_c64_any(p->args.pp.n, a, l, p->op, p->strided, p->d.kernel_op);
+    e = launch_fixed_c64_any(p->args.pp.n, a, l, p->op, p->strided, p->d.kernel_op, variant);
     if (e != cudaSuccess) return cuda_fail(e, "FFT launch");
     return VDX_OK;
   }
   switch (p->store) {
-    case ST_C64: e = launch_fft<Cx<float>, float>(a, l, p->op, p->strided, p->d.kernel_op); break;
-    case ST_C32: e = launch_fft<c32s, float>(a, l, p->op, p->strided, p->d.kernel_op); break;
-    case ST_BF16: e = launch_fft<bf16c, float>(a, l, p->op, p->strided, p->d.kernel_op); break;
-    case ST_C128: e = launch_fft<Cx<double>, double>(a, l, p->op, p->strided, p->d.kernel_op); break;
+    case ST_C64: e = launch_fft<Cx<float>, float>(a, l, p->op, p->strided, p->d.kernel_op, variant); break;
+    case ST_C32: e = launch_fft<c32s, float>(a, l, p->op, p->strided, p->d.kernel_op, variant); break;
+    case ST_BF16: e = launch_fft<bf16c, float>(a, l, p->op, p->strided, p->d.kernel_op, variant); break;
+    case ST_C128: e = launch_fft<Cx<double>, double>(a, l, p->op, p->strided, p->d.kernel_op, variant); break;
     default: return fail(VDX_ERR_INVALID, "bad plan storage type");
   }
   if (e != cudaSuccess) return cuda_fail(e, "FFT launch");
+  return VDX_OK;
+}
+
+}  // namespace
+
+int vdx_fft_exec(const vdx_plan* p, const void* in, void* out, const void* kernel, void* stream) {
+  return exec_plan(p, in, out, kernel, nullptr, stream);
+}
+
+int vdx_fft_exec_ops(const vdx_plan* p, const void* in, void* out, const void* kernel, const vdx_exec_ops* ops,
+                     void* stream) {
+  return exec_plan(p, in, out, kernel, ops, stream);
+}
+
+int vdx_fft_plan_ctas(const vdx_plan* p, int64_t* ctas) {
+  if (!p || !ctas) return fail(VDX_ERR_INVALID, "plan and ctas must be non-NULL");
+  *ctas = (int64_t)p->launch.grid.x;
   return VDX_OK;
 }
 

@@ -38,16 +38,17 @@ struct MaxE<double> {
 enum Op { OP_C2C_FWD, OP_C2C_INV, OP_CONV, OP_R2C_EVEN, OP_C2R_EVEN, OP_R2C_ODD, OP_C2R_ODD };
 
 template <class S, class Re>
-cudaError_t launch_fft(const FftArgs& a, const Launch& l, int op, bool strided, int kop);
+cudaError_t launch_fft(const FftArgs& a, const Launch& l, int op, bool strided, int kop, int variant);
 
 cudaError_t launch_twiddle(void* tab, int count, int den, bool f64, cudaStream_t s);
 
 // complex64 kernels specialised at compile time for power-of-two n in
 // [16, 16384] (radix-16 passes, n/16 threads per transform)
 template <int N>
-cudaError_t launch_fixed_c64(const FftArgs& a, const Launch& l, int op, bool strided, int kop);
+cudaError_t launch_fixed_c64(const FftArgs& a, const Launch& l, int op, bool strided, int kop, int variant);
 bool has_fixed_c64(int n);
-cudaError_t launch_fixed_c64_any(int n, const FftArgs& a, const Launch& l, int op, bool strided, int kop);
+cudaError_t launch_fixed_c64_any(int n, const FftArgs& a, const Launch& l, int op, bool strided, int kop,
+                                 int variant);
 
 // Opt a kernel into more than 48 KB of dynamic shared memory once.
 template <class K>

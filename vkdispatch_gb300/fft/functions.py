@@ -135,7 +135,7 @@ def fft(
         ax,
         kind,
         inverse,
-        normalize_inverse,
+        bool(inverse and normalize_inverse),
         out_t.vdx_code,
         _compute_code(out_t, compute),
         _signal(input_signal_range, N),

@@ -31,6 +31,15 @@ class Plan:
     def exec(self, in_ptr: int, out_ptr: int, ker_ptr: Optional[int], stream: int) -> None:
         L.check(L.lib().vdx_fft_exec(self.handle, in_ptr, out_ptr, ker_ptr, stream), "FFT exec")
 
+    def exec_ops(self, in_ptr: int, out_ptr: int, ker_ptr: Optional[int], ops: L.ExecOps, stream: int) -> None:
+        L.check(L.lib().vdx_fft_exec_ops(self.handle, in_ptr, out_ptr, ker_ptr, ctypes.byref(ops), stream),
+                "FFT exec")
+
+    def ctas(self) -> int:
+        c = ctypes.c_int64()
+        L.check(L.lib().vdx_fft_plan_ctas(self.handle, ctypes.byref(c)), "FFT plan ctas")
+        return int(c.value)
+
     def __del__(self):
         try:
             if self.handle:
