@@ -145,6 +145,15 @@ int vdx_fft_exec_ops(const vdx_plan* plan, const void* in, void* out, const void
 /* Number of CTAs one vdx_fft_exec of this plan launches. */
 int vdx_fft_plan_ctas(const vdx_plan* plan, int64_t* ctas);
 
+/*
+ * Element-wise conversion of `count` elements between VDX_C64, VDX_C128,
+ * VDX_C32, VDX_BF16X2, VDX_F32 and VDX_F64 (real -> complex: imaginary part
+ * 0; complex -> real: real part).  The load and store ends of the map hooks
+ * that change precision or read/write real buffers (vkdispatch/fft/
+ * global_memory_iterators.py:71-92, 197-229 with a cast in the map).
+ */
+int vdx_convert(const void* src, int src_type, void* dst, int dst_type, int64_t count, void* stream);
+
 /* reduction operations (vkdispatch/reduce/operations.py:17-66) */
 #define VDX_RED_ADD 0
 #define VDX_RED_MUL 1

@@ -134,3 +134,39 @@ def test_string_annotations_of_enclosing_locals_resolve_by_name():
     mf = vd.reduce.MappingFunction(ns["outer"]())
     assert mf.input_dtypes() == [vd.complex64]
     assert mf.return_type == vd.float32
+
+
+def test_output_map_requires_input_buffer_after_map_args():
+    from vkdispatch_gb300.fft.functions import _split_buffers
+
+    class Fake:
+        def __init__(self, t):
+            self.var_type = t
+
+    om = vd.map(lambda b: None, input_types=[vc.Buffer[vd.complex64], vc.Buffer[vd.float32]])
+    outs, ins, _ = _split_buffers((Fake(vd.complex64), Fake(vd.float32), Fake(vd.complex128)), None, om)
+    assert len(outs) == 2 and ins[0].var_type == vd.complex128
+    om1 = vd.map(lambda b: None, input_types=[vc.Buffer[vd.complex64]])
+    with pytest.raises(ValueError, match="input buffer argument must be provided"):
+        _split_buffers((Fake(vd.complex64),), None, om1)
+
+
+def test_map_classification_menu():
+    from vkdispatch_gb300.fft import maps as M
+
+    def rin(buffer: vc.Buffer[vd.float32]):
+        op = vd.fft.read_op()
+        op.register.real = vc.to_dtype(vd.float32, buffer[op.io_index])
+        op.register.imag = vc.to_dtype(vd.float32, 0)
+
+    def cout(buffer: vc.Buffer[vd.complex128]):
+        vd.fft.write_op().write_to_buffer(buffer)
+
+    def nothing():
+        return
+
+    assert M.classify_input(vd.map(rin)).kind == "real"
+    assert M.classify_output(vd.map(cout)).var_type == vd.complex128
+    assert M.classify_kernel(vd.map(nothing)).kind == "identity"
+    with pytest.raises(ValueError):
+        vd.fft.read_op()  # only valid while a map function is traced

@@ -15,7 +15,7 @@ from . import fft  # noqa: F401
 from . import reduce  # noqa: F401
 from ._lib import lib as _load_lib  # noqa: F401
 from .buffer import Buffer, RFFTBuffer, asbuffer, asrfftbuffer, from_cuda_array  # noqa: F401
-from .dtype import (  # noqa: F401
+from .dtypes import (  # noqa: F401
     bfloat16,
     complex32,
     complex64,

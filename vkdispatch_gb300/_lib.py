@@ -21,6 +21,10 @@ VDX_ERR_NOMEM = 4
 # element types
 VDX_C64, VDX_C32, VDX_C128, VDX_BF16X2, VDX_F32, VDX_F64, VDX_I32, VDX_U32 = range(8)
 
+
+def convert(src_ptr: int, src_type: int, dst_ptr: int, dst_type: int, count: int, stream: int) -> None:
+    check(lib().vdx_convert(src_ptr, src_type, dst_ptr, dst_type, count, stream), "convert")
+
 # transform kinds
 VDX_KIND_C2C, VDX_KIND_R2C, VDX_KIND_C2R, VDX_KIND_CONV = range(4)
 VDX_KOP_MUL_CONJ, VDX_KOP_MUL = range(2)
@@ -42,6 +46,7 @@ EXPORTED = (
     "vdx_reduce_noalloc",
     "vdx_fft_exec_ops",
     "vdx_fft_plan_ctas",
+    "vdx_convert",
 )
 VDX_REDUCE_NOALLOC_SCRATCH_BYTES = 1048576
 
@@ -110,6 +115,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.vdx_fft_exec_ops.argtypes = [vp, vp, vp, vp, ctypes.POINTER(ExecOps), vp]
     lib.vdx_fft_plan_ctas.restype = i32
     lib.vdx_fft_plan_ctas.argtypes = [vp, ctypes.POINTER(i64)]
+    lib.vdx_convert.restype = i32
+    lib.vdx_convert.argtypes = [vp, i32, vp, i32, i64, vp]
     lib.vdx_reduce_noalloc.restype = i32
     lib.vdx_reduce_noalloc.argtypes = [i32, i32, i32, vp, i64, i64, vp, vp]
 

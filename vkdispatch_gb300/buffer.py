@@ -15,7 +15,7 @@ from typing import Optional, Tuple
 import numpy as np
 import torch
 
-from . import dtype as dt
+from . import dtypes as dt
 
 MAX_ELEMENTS = 2**30  # the reference caps buffers at 2^30 elements (buffer.py:86-87)
 

@@ -11,7 +11,7 @@ outside the menu raises NotImplementedError naming the function.
 
 from __future__ import annotations
 
-from . import dtype as dt
+from . import dtypes as dt
 
 f16, f32, f64 = dt.float16, dt.float32, dt.float64
 i32, u32 = dt.int32, dt.uint32
@@ -142,3 +142,25 @@ def min(a, b):  # noqa: A001
 
 def max(a, b):  # noqa: A001
     return Sym("max", a, b)
+
+
+# --- used by FFT map hooks (vkdispatch_gb300/fft/maps.py traces them) -------
+def to_dtype(var_type, *args):
+    """Cast (one argument) or build a value of var_type from components."""
+    if len(args) == 1:
+        return Sym("cast", args[0])
+    return Sym("make", *args)
+
+
+def to_complex(x):
+    return Sym("to_complex", x)
+
+
+def mult_complex(a, b):
+    return Sym("cmul", a, b)
+
+
+def new_register(var_type, *args, var_name=None):
+    from .fft import maps
+
+    return maps.new_trace_register(var_type)

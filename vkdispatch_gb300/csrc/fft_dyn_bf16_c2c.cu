@@ -1,0 +1,9 @@
+// Runtime-plan C2C kernels for storage bf16c with float butterflies.
+#include "fft_launch.cuh"
+
+namespace vdx {
+template <>
+cudaError_t launch_dyn_c2c<bf16c, float>(const FftArgs& a, const Launch& l, int op, bool strided, int variant) {
+  return launch_c2c_any<DynPlan<MaxE<float>::value>, bf16c, float>(a, l, op, strided, variant);
+}
+}  // namespace vdx

@@ -126,13 +126,10 @@ __device__ __forceinline__ void radix_dispatch(int R, F&& f) {
     case 3: f(IC<3>{}); break;
     case 4: f(IC<4>{}); break;
     case 5: f(IC<5>{}); break;
-    case 6: f(IC<6>{}); break;
     case 7: f(IC<7>{}); break;
     case 8: f(IC<8>{}); break;
     case 9: f(IC<9>{}); break;
-    case 10: f(IC<10>{}); break;
     case 11: f(IC<11>{}); break;
-    case 12: f(IC<12>{}); break;
     case 13: f(IC<13>{}); break;
     case 16: f(IC<16>{}); break;
     default: break;
@@ -214,16 +211,17 @@ __device__ __forceinline__ void run_passes(Cx<Re>* v, const PassPlan& pp, bool r
   for (int q = 0; q < P; ++q) {
     const int p = reversed ? P - 1 - q : q;
     const int R = pp.radix[p];
+    const bool more = q + 1 < P;
+    // one radix dispatch per pass covers the butterflies and the scatter
     radix_dispatch(R, [&](auto rc) {
       constexpr int RR = decltype(rc)::value;
       butterflies<RR, MAXE, INV, Re>(v, n / RR, T, t, ns, n, tw);
-    });
-    if (q + 1 < P) {
-      __syncthreads();
-      radix_dispatch(R, [&](auto rc) {
-        constexpr int RR = decltype(rc)::value;
+      if (more) {
+        __syncthreads();
         scatter<RR, MAXE, Re>(v, n / RR, T, t, ns, [&](int pos, Cx<Re> val) { sm[pl.sidx(pp, pos)] = val; });
-      });
+      }
+    });
+    if (more) {
       __syncthreads();
       const int R2 = pp.radix[reversed ? P - 2 - q : q + 1];
       radix_dispatch(R2, [&](auto rc) {
@@ -234,7 +232,6 @@ __device__ __forceinline__ void run_passes(Cx<Re>* v, const PassPlan& pp, bool r
     ns *= R;
   }
 }
-
 
 // ---------------------------------------------------------------------------
 // plan policies: how the kernels below learn n, T and the radix passes.

@@ -25,54 +25,97 @@ cudaError_t launch_c2c(const FftArgs& a, const Launch& l, bool strided, int vari
 }
 
 // convolution with optional spectrum output (complex64 only): variant 0 =
-// none, 1 = write S, 2 = write aux * conj(S) * scale
-template <class Plan, int KOP, class S, class Re>
-cudaError_t launch_conv(const FftArgs& a, const Launch& l, bool strided, int variant) {
-  if constexpr (std::is_same<S, Cx<float>>::value) {
-    if (variant == 1) {
-      if (strided) return enqueue(k_conv<Plan, true, S, S, Re, KOP, 1>, l, a);
-      return enqueue(k_conv<Plan, false, S, S, Re, KOP, 1>, l, a);
-    }
-    if (variant == 2) {
-      if (strided) return enqueue(k_conv<Plan, true, S, S, Re, KOP, 2>, l, a);
-      return enqueue(k_conv<Plan, false, S, S, Re, KOP, 2>, l, a);
-    }
+// none, 1 = write S (used with the conjugate product of a forward
+// convolution), 2 = write aux * conj(S) * scale (used with the plain product
+// of its adjoint); the plain product (KOP 1) exists for complex64 only
+template <class Plan, int KOP, bool STRIDED, class S, class Re>
+cudaError_t launch_conv_layout(const FftArgs& a, const Launch& l, int variant) {
+  constexpr bool C64 = std::is_same<S, Cx<float>>::value;
+  if constexpr (C64 && KOP == 0) {
+    if (variant == 1) return enqueue(k_conv<Plan, STRIDED, S, S, Re, 0, 1>, l, a);
+  }
+  if constexpr (C64 && KOP == 1) {
+    if (variant == 2) return enqueue(k_conv<Plan, STRIDED, S, S, Re, 1, 2>, l, a);
   }
   if (variant != 0) return cudaErrorInvalidValue;
-  if (strided) return enqueue(k_conv<Plan, true, S, S, Re, KOP>, l, a);
-  return enqueue(k_conv<Plan, false, S, S, Re, KOP>, l, a);
+  if constexpr (KOP == 1 && !C64) return cudaErrorInvalidValue;
+  else return enqueue(k_conv<Plan, STRIDED, S, S, Re, KOP>, l, a);
+}
+
+template <class Plan, int KOP, class S, class Re>
+cudaError_t launch_conv(const FftArgs& a, const Launch& l, bool strided, int variant) {
+  if (strided) return launch_conv_layout<Plan, KOP, true, S, Re>(a, l, variant);
+  return launch_conv_layout<Plan, KOP, false, S, Re>(a, l, variant);
 }
 
 // Launches `op` with plan policy Plan (DynPlan or a compile-time FixPlan).
-template <class Plan, class S, class Re, bool WITH_ODD>
-cudaError_t launch_with_plan(const FftArgs& a, const Launch& l, int op, bool strided, int kop, int variant) {
-  if (variant != 0 && op != OP_C2C_FWD && op != OP_C2C_INV && op != OP_CONV) return cudaErrorInvalidValue;
+template <class Plan, class S, class Re>
+cudaError_t launch_real(const FftArgs& a, const Launch& l, int op, bool with_odd) {
   switch (op) {
-    case OP_C2C_FWD:
-      return launch_c2c<Plan, false, S, Re>(a, l, strided, variant);
-    case OP_C2C_INV:
-      return launch_c2c<Plan, true, S, Re>(a, l, strided, variant);
-    case OP_CONV:
-      if (kop == 0) return launch_conv<Plan, 0, S, Re>(a, l, strided, variant);
-      return launch_conv<Plan, 1, S, Re>(a, l, strided, variant);
     case OP_R2C_EVEN:
       return enqueue(k_r2c_even<Plan, S, Re>, l, a);
     case OP_C2R_EVEN:
       return enqueue(k_c2r_even<Plan, S, Re>, l, a);
     case OP_R2C_ODD:
-      if constexpr (WITH_ODD) return enqueue(k_real_odd<Plan, false, S, Re>, l, a);
+      if (with_odd) return enqueue(k_real_odd<Plan, false, S, Re>, l, a);
       return cudaErrorInvalidValue;
     case OP_C2R_ODD:
-      if constexpr (WITH_ODD) return enqueue(k_real_odd<Plan, true, S, Re>, l, a);
+      if (with_odd) return enqueue(k_real_odd<Plan, true, S, Re>, l, a);
       return cudaErrorInvalidValue;
     default:
       return cudaErrorInvalidValue;
   }
 }
 
+template <class Plan, class S, class Re>
+cudaError_t launch_c2c_any(const FftArgs& a, const Launch& l, int op, bool strided, int variant) {
+  if (op == OP_C2C_FWD) return launch_c2c<Plan, false, S, Re>(a, l, strided, variant);
+  return launch_c2c<Plan, true, S, Re>(a, l, strided, variant);
+}
+
+template <class Plan, class S, class Re>
+cudaError_t launch_conv_any(const FftArgs& a, const Launch& l, bool strided, int kop, int variant) {
+  if (kop == 0) return launch_conv<Plan, 0, S, Re>(a, l, strided, variant);
+  return launch_conv<Plan, 1, S, Re>(a, l, strided, variant);
+}
+
+// The runtime-plan kernels of one storage type are split over three
+// translation units (C2C, convolution, real) so they compile in parallel.
+template <class S, class Re>
+cudaError_t launch_dyn_c2c(const FftArgs& a, const Launch& l, int op, bool strided, int variant);
+template <class S, class Re>
+cudaError_t launch_dyn_conv(const FftArgs& a, const Launch& l, bool strided, int kop, int variant);
+template <class S, class Re, bool STRIDED>
+cudaError_t launch_dyn_conv_layout(const FftArgs& a, const Launch& l, int kop, int variant);
+template <class S, class Re>
+cudaError_t launch_dyn_real(const FftArgs& a, const Launch& l, int op);
+
+template <class Plan, class S, class Re, bool WITH_ODD>
+cudaError_t launch_with_plan(const FftArgs& a, const Launch& l, int op, bool strided, int kop, int variant) {
+  if (variant != 0 && op != OP_C2C_FWD && op != OP_C2C_INV && op != OP_CONV) return cudaErrorInvalidValue;
+  switch (op) {
+    case OP_C2C_FWD:
+    case OP_C2C_INV:
+      return launch_c2c_any<Plan, S, Re>(a, l, op, strided, variant);
+    case OP_CONV:
+      return launch_conv_any<Plan, S, Re>(a, l, strided, kop, variant);
+    default:
+      return launch_real<Plan, S, Re>(a, l, op, WITH_ODD);
+  }
+}
+
 template <class S, class Re>
 cudaError_t launch_fft(const FftArgs& a, const Launch& l, int op, bool strided, int kop, int variant) {
-  return launch_with_plan<DynPlan<MaxE<Re>::value>, S, Re, true>(a, l, op, strided, kop, variant);
+  if (variant != 0 && op != OP_C2C_FWD && op != OP_C2C_INV && op != OP_CONV) return cudaErrorInvalidValue;
+  switch (op) {
+    case OP_C2C_FWD:
+    case OP_C2C_INV:
+      return launch_dyn_c2c<S, Re>(a, l, op, strided, variant);
+    case OP_CONV:
+      return launch_dyn_conv<S, Re>(a, l, strided, kop, variant);
+    default:
+      return launch_dyn_real<S, Re>(a, l, op);
+  }
 }
 
 template <int N>

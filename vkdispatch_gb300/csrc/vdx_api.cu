@@ -68,8 +68,7 @@ int get_table(int dev, int count, int den, bool f64, void** out) {
 // radix factorisation
 // ---------------------------------------------------------------------------
 // Splits n into passes: radix 16 for each 2^4, the leftover power of two
-// folded into an odd radix when possible (6, 10, 12), 9 for pairs of 3s, then
-// 3, 5, 7, 11, 13.  Fails for primes above 13, the reference's largest
+// (2, 4 or 8), 9 for pairs of 3s, then 3, 5, 7, 11, 13.  Fails for primes above 13, the reference's largest
 // supported prime (vkdispatch/fft/prime_utils.py:9-10).
 bool factor_radices(int n, int maxe, std::vector<int>& radices, std::string& why) {
   radices.clear();
@@ -103,30 +102,11 @@ bool factor_radices(int n, int maxe, std::vector<int>& radices, std::string& why
     radices.push_back(9);
     cnt[3] -= 2;
   }
-  if (cnt[3] == 1) {
-    if (rem2 == 2 && maxe >= 6) {
-      radices.push_back(6);
-      rem2 = 1;
-    } else if (rem2 == 4 && maxe >= 12) {
-      radices.push_back(12);
-      rem2 = 1;
-    } else {
-      radices.push_back(3);
-    }
-    cnt[3] = 0;
-  }
   while (cnt[3] > 0) {
     radices.push_back(3);
     --cnt[3];
   }
-  for (int i = 0; i < cnt[5]; ++i) {
-    if (rem2 == 2 && maxe >= 10) {
-      radices.push_back(10);
-      rem2 = 1;
-    } else {
-      radices.push_back(5);
-    }
-  }
+  for (int i = 0; i < cnt[5]; ++i) radices.push_back(5);
   for (int p : {7, 11, 13})
     for (int i = 0; i < cnt[p]; ++i) radices.push_back(p);
   if (rem2 > 1) radices.push_back(rem2);
@@ -241,6 +221,8 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
     if (d.kernel_type != d.io_type) return fail(VDX_ERR_UNSUPPORTED, "kernel_type must equal io_type");
     if (d.kernel_op != VDX_KOP_MUL_CONJ && d.kernel_op != VDX_KOP_MUL)
       return fail(VDX_ERR_INVALID, "unknown kernel_op");
+    if (d.kernel_op == VDX_KOP_MUL && st != ST_C64)
+      return fail(VDX_ERR_UNSUPPORTED, "VDX_KOP_MUL convolutions need complex64 storage");
   }
   if (real && (st == ST_BF16)) return fail(VDX_ERR_UNSUPPORTED, "real transforms support complex64/complex32/complex128");
 

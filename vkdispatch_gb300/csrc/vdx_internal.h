@@ -39,6 +39,12 @@ enum Op { OP_C2C_FWD, OP_C2C_INV, OP_CONV, OP_R2C_EVEN, OP_C2R_EVEN, OP_R2C_ODD,
 
 template <class S, class Re>
 cudaError_t launch_fft(const FftArgs& a, const Launch& l, int op, bool strided, int kop, int variant);
+template <class S, class Re>
+cudaError_t launch_dyn_c2c(const FftArgs& a, const Launch& l, int op, bool strided, int variant);
+template <class S, class Re>
+cudaError_t launch_dyn_conv(const FftArgs& a, const Launch& l, bool strided, int kop, int variant);
+template <class S, class Re>
+cudaError_t launch_dyn_real(const FftArgs& a, const Launch& l, int op);
 
 cudaError_t launch_twiddle(void* tab, int count, int den, bool f64, cudaStream_t s);
 

@@ -21,4 +21,5 @@ from .functions import (  # noqa: F401
     rfft3,
     transpose,
 )
+from .maps import read_op, write_op  # noqa: F401
 from .plan import get_plan  # noqa: F401

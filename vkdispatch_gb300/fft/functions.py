@@ -14,10 +14,11 @@ from typing import Optional, Tuple, Union
 import numpy as np
 
 from .. import _lib as L
-from .. import dtype as dt
+from .. import dtypes as dt
 from .. import graph as G
 from ..buffer import Buffer, RFFTBuffer
 from . import plan as P
+from .maps import read_op, write_op  # noqa: F401
 
 _PRECISION_ORDER = (dt.complex32, dt.complex64, dt.complex128)
 
@@ -58,13 +59,107 @@ def _norm_axis(axis: Optional[int], ndim: int) -> int:
     return axis
 
 
-def _no_maps(**maps) -> None:
-    for name, m in maps.items():
-        if m is not None:
-            raise NotImplementedError(
-                f"{name} is not in the supported map menu of this build (use the io/compute dtype arguments, "
-                "input_signal_range, or kernel_inner_only instead)"
-            )
+_TORCH_OF = {"complex64": "complex64", "complex128": "complex128"}
+
+
+def _native_pair(io_t: dt.dtype, compute: dt.dtype) -> bool:
+    """(storage, compute) pairs the kernels run directly."""
+    c = _compute_code(io_t, compute)
+    if io_t == dt.complex128:
+        return c == L.VDX_C128
+    return c == L.VDX_C64 and io_t in (dt.complex64, dt.complex32, dt.complexbf16)
+
+
+def _compute_torch(compute: dt.dtype):
+    import torch
+
+    return torch.complex128 if _compute_code(None, compute) == L.VDX_C128 else torch.complex64
+
+
+def _split_buffers(buffers, input_map, output_map, kernel_map=None, conv=False):
+    """The reference's argument order: output-map buffers (or the output
+    buffer), input-map buffers (or, with only an output map, one input buffer),
+    kernel-map buffers (or the kernel buffer) -- vkdispatch/fft/
+    io_manager.py:58-105."""
+    n_out = len(output_map.buffer_types) if output_map is not None else 1
+    outs = list(buffers[:n_out])
+    rest = list(buffers[n_out:])
+    if input_map is not None:
+        n_in = len(input_map.buffer_types)
+        ins, rest = rest[:n_in], rest[n_in:]
+    elif output_map is not None:
+        if not rest:
+            raise ValueError("When output_map is used without input_map, an input buffer argument must be provided "
+                             "after output_map arguments")
+        ins, rest = rest[:1], rest[1:]
+    else:
+        ins = None
+    if conv:
+        n_k = len(kernel_map.buffer_types) if kernel_map is not None else 1
+        kers, rest = rest[:n_k], rest[n_k:]
+    else:
+        kers = []
+    return outs, ins, kers
+
+
+def _io_ends(outs, ins, input_map, output_map):
+    """(out buffer, out kind, in buffer, in kind) after map recognition."""
+    from . import maps as M
+
+    if output_map is not None:
+        om = M.classify_output(output_map)
+        out_buf, out_kind = outs[om.buffer], om.kind
+        if out_buf.var_type != om.var_type:
+            raise ValueError(f"output map buffer type {out_buf.var_type.name} does not match its annotation")
+    else:
+        out_buf, out_kind = outs[0], "complex"
+    if input_map is not None:
+        im = M.classify_input(input_map)
+        in_buf, in_kind = ins[im.buffer], im.kind
+        if in_buf.var_type != im.var_type:
+            raise ValueError(f"input map buffer type {in_buf.var_type.name} does not match its annotation")
+    elif ins is not None:
+        in_buf, in_kind = ins[0], "complex"
+    else:
+        in_buf, in_kind = out_buf, out_kind
+    return out_buf, out_kind, in_buf, in_kind
+
+
+def _staged(plan_fn, out_buf, out_kind, in_buf, in_kind, shape, compute, graph, ker=None, keep=(), pre=None):
+    """Runs a compute-precision plan between buffers of other types: the
+    input is converted into a compute-type buffer unless it already is one,
+    the plan runs out of place into the output (or a staging buffer), and the
+    staging buffer is converted into the output's type."""
+    import torch
+
+    ct = _compute_torch(compute)
+    code = L.VDX_C128 if ct == torch.complex128 else L.VDX_C64
+    count = int(np.prod(shape))
+    in_direct = in_kind == "complex" and in_buf.var_type.vdx_code == code
+    out_direct = out_kind == "complex" and out_buf.var_type.vdx_code == code
+    stage_in = None if in_direct else torch.empty(count, dtype=ct, device=in_buf.tensor.device)
+    stage_out = None if out_direct else torch.empty(count, dtype=ct, device=out_buf.tensor.device)
+    plan = plan_fn(code)
+    in_ptr, in_type = in_buf.ptr, in_buf.var_type.vdx_code
+    out_ptr, out_type = out_buf.ptr, out_buf.var_type.vdx_code
+    if in_kind == "real":
+        in_type = L.VDX_F32 if in_buf.var_type == dt.float32 else L.VDX_F64
+    if out_kind == "real":
+        out_type = L.VDX_F32 if out_buf.var_type == dt.float32 else L.VDX_F64
+
+    def launch(s):
+        if pre is not None:
+            pre(s)
+        src = in_ptr
+        if stage_in is not None:
+            L.convert(in_ptr, in_type, stage_in.data_ptr(), code, count, s)
+            src = stage_in.data_ptr()
+        dst = out_ptr if stage_out is None else stage_out.data_ptr()
+        plan.exec(src, dst, ker, s)
+        if stage_out is not None:
+            L.convert(stage_out.data_ptr(), code, out_ptr, out_type, count, s)
+
+    _record(graph, launch, (in_buf, out_buf, stage_in, stage_out) + tuple(keep))
 
 
 def _signal(sr, N: int) -> Optional[Tuple[int, int]]:
@@ -103,7 +198,28 @@ def fft(
         raise ValueError("At least one buffer must be provided")
     if input_map is None and output_map is None and len(buffers) != 1:
         raise ValueError("fft() expects exactly one buffer unless input_map/output_map are used")
-    _no_maps(input_map=input_map, output_map=output_map)
+    if input_map is not None or output_map is not None:
+        if r2c:
+            raise NotImplementedError("map hooks on real (r2c) transforms are not in the supported menu")
+        if input_map is not None and input_type is not None:
+            raise ValueError("input_type cannot be provided when input_map is used")
+        if output_map is not None and output_type is not None:
+            raise ValueError("output_type cannot be provided when output_map is used")
+        outs, ins, _ = _split_buffers(buffers, input_map, output_map)
+        out_buf, out_kind, in_buf, in_kind = _io_ends(outs, ins, input_map, output_map)
+        io = []
+        if output_map is None:
+            io.append(out_buf.var_type)
+        if input_map is None:
+            io.append(in_buf.var_type if input_type is None else input_type)
+        compute = resolve_compute_precision(io, compute_type)
+        shape = tuple(int(x) for x in (buffer_shape if buffer_shape is not None else buffers[0].shape))
+        ax = _norm_axis(axis, len(shape))
+        sr = _signal(input_signal_range, shape[ax])
+        _staged(lambda code: P.get_plan(shape, ax, L.VDX_KIND_C2C, inverse, bool(inverse and normalize_inverse), code,
+                                        code, sr),
+                out_buf, out_kind, in_buf, in_kind, shape, compute, graph)
+        return
     buf = buffers[0]
     if buffer_shape is None:
         buffer_shape = buf.shape
@@ -119,6 +235,12 @@ def fft(
     compute = resolve_compute_precision([out_t, in_t], compute_type)
     ax = _norm_axis(axis, len(buffer_shape))
     N = buffer_shape[ax]
+    if not r2c and not _native_pair(out_t, compute):
+        # e.g. complex64 storage with complex128 compute: stage through the compute type
+        _staged(lambda code: P.get_plan(buffer_shape, ax, L.VDX_KIND_C2C, inverse, bool(inverse and normalize_inverse),
+                                        code, code, _signal(input_signal_range, N)),
+                buf, "complex", buf, "complex", buffer_shape, compute, graph)
+        return
     if r2c:
         if ax != len(buffer_shape) - 1:
             raise ValueError("R2C io only supported for contiguous data")
@@ -269,9 +391,12 @@ def convolve(
         raise ValueError("At least one buffer must be provided")
     if kernel_map is None and len(buffers) < 2:
         raise ValueError("convolve() requires at least an output buffer and kernel buffer")
-    _no_maps(input_map=input_map, output_map=output_map, kernel_map=kernel_map)
     if kernel_num != 1:
         raise NotImplementedError("kernel_num > 1 is not supported by this build")
+    if input_map is not None or output_map is not None or kernel_map is not None:
+        _convolve_mapped(buffers, kernel_map, buffer_shape, graph, axis, normalize, kernel_inner_only, input_map,
+                         output_map, compute_type, input_signal_range)
+        return
     buf, ker = buffers[0], buffers[1]
     if buffer_shape is None:
         buffer_shape = buf.shape
@@ -312,6 +437,70 @@ def convolve(
         print(plan.describe())
     ptr, kptr = buf.ptr, ker.ptr
     _record(graph, lambda s: plan.exec(ptr, ptr, kptr, s), (buf, ker))
+
+
+def _convolve_mapped(buffers, kernel_map, buffer_shape, graph, axis, normalize, kernel_inner_only, input_map,
+                     output_map, compute_type, input_signal_range):
+    import torch
+
+    from . import maps as M
+
+    outs, ins, kers = _split_buffers(buffers, input_map, output_map, kernel_map, conv=True)
+    out_buf, out_kind, in_buf, in_kind = _io_ends(outs, ins, input_map, output_map)
+    km = M.classify_kernel(kernel_map) if kernel_map is not None else M.KernelMap("conj_mul", 0, kers[0].var_type)
+    io = []
+    if output_map is None:
+        io.append(out_buf.var_type)
+    if input_map is None:
+        io.append(in_buf.var_type)
+    if kernel_map is None:
+        io.append(kers[0].var_type)
+    compute = resolve_compute_precision(io, compute_type)
+    shape = tuple(int(x) for x in (buffer_shape if buffer_shape is not None else buffers[0].shape))
+    ax = _norm_axis(axis, len(shape))
+    sr = _signal(input_signal_range, shape[ax])
+    total, slab = int(np.prod(shape)), int(np.prod(shape[ax:]))
+    if km.kind == "identity":
+        # no spectrum operation: the forward and inverse transforms cancel up to 1/N
+        def plan_fn(code):
+            class _Pair:
+                def __init__(self):
+                    self.f = P.get_plan(shape, ax, L.VDX_KIND_C2C, False, False, code, code, sr)
+                    self.i = P.get_plan(shape, ax, L.VDX_KIND_C2C, True, bool(normalize), code, code)
+
+                def exec(self, src, dst, ker, s):
+                    self.f.exec(src, dst, None, s)
+                    self.i.exec(dst, dst, None, s)
+
+            return _Pair()
+
+        _staged(plan_fn, out_buf, out_kind, in_buf, in_kind, shape, compute, graph)
+        return
+    kbuf = kers[km.buffer]
+    ct = _compute_torch(compute)
+    code = L.VDX_C128 if ct == torch.complex128 else L.VDX_C64
+    pre = None
+    if kbuf.var_type.vdx_code == code and km.kind != "real_scale":
+        kptr, keep = kbuf.ptr, (kbuf,)
+    else:
+        # real scale buffers (or other precisions) become a compute-type
+        # spectrum, converted inside the launch so recorded graphs see the
+        # kernel buffer's contents at submit time
+        kt = torch.empty(kbuf.size, dtype=ct, device=kbuf.tensor.device)
+        src_type = {dt.float32: L.VDX_F32, dt.float64: L.VDX_F64}.get(kbuf.var_type, kbuf.var_type.vdx_code)
+        kptr, keep = kt.data_ptr(), (kbuf, kt)
+        kb_ptr, kb_n = kbuf.ptr, kbuf.size
+
+        def pre(s):
+            L.convert(kb_ptr, src_type, kptr, code, kb_n, s)
+    kop = L.VDX_KOP_MUL_CONJ if km.kind == "conj_mul" else L.VDX_KOP_MUL
+    if kop == L.VDX_KOP_MUL and code != L.VDX_C64:
+        raise NotImplementedError("plain-product kernel maps need complex64 compute")
+    broadcast = bool(kernel_inner_only) or (kbuf.size < total and kbuf.size >= slab)
+    if not broadcast and kbuf.size < total:
+        raise ValueError(f"kernel buffer of {kbuf.size} elements is smaller than the signal ({total})")
+    _staged(lambda c: P.get_plan(shape, ax, L.VDX_KIND_CONV, False, normalize, c, c, sr, kop, c, broadcast),
+            out_buf, out_kind, in_buf, in_kind, shape, compute, graph, ker=kptr, keep=keep, pre=pre)
 
 
 def convolve2D(buffer: Buffer, kernel: Buffer, kernel_map=None, buffer_shape=None, graph=None, print_shader=False,

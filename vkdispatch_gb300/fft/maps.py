@@ -1,0 +1,216 @@
+"""Map hooks for FFTs and convolutions: `vd.fft.read_op()` / `write_op()` and
+the recognition of user map functions (vkdispatch/fft/io_manager.py:23-37,
+vkdispatch/shader/map.py:10-68).
+
+A map function is called once with symbolic buffers and read/write-op
+objects that record what it does.  The record is matched against the menu
+libvdx implements; anything else raises NotImplementedError naming the map.
+
+  input maps   read_op().read_from_buffer(buf)           complex load of buf's type
+               register.real = buf[io_index]; .imag = 0  real load (imaginary 0)
+  output maps  write_op().write_to_buffer(buf)           complex store in buf's type
+               buf[io_index] = write_op().register.real  real-part store
+  kernel maps  read into a register k, register *= conj(k)   conjugate product (the default)
+               read into a register k, register *= k         plain product
+               register *= to_complex(scale[io_index])       real scale buffer
+               (empty body)                                  no spectrum operation
+"""
+
+from __future__ import annotations
+
+import threading
+from dataclasses import dataclass
+from typing import List, Optional
+
+from .. import codegen as vc
+from .. import dtypes as dt
+
+_tls = threading.local()
+
+
+class TraceRegister:
+    def __init__(self, name: str, events: list):
+        object.__setattr__(self, "_name", name)
+        object.__setattr__(self, "_events", events)
+
+    @property
+    def real(self):
+        return vc.Sym("reg_real", self._name)
+
+    @real.setter
+    def real(self, value):
+        self._events.append(("set_real", self._name, value))
+
+    @property
+    def imag(self):
+        return vc.Sym("reg_imag", self._name)
+
+    @imag.setter
+    def imag(self, value):
+        self._events.append(("set_imag", self._name, value))
+
+    def __setitem__(self, key, value):
+        self._events.append(("set", self._name, value))
+
+    def conjugate(self):
+        return vc.Sym("conj", vc.Sym("reg", self._name))
+
+    @property
+    def var_type(self):
+        return dt.complex64
+
+    def __repr__(self):
+        return f"reg({self._name})"
+
+
+class _TraceBuffer:
+    def __init__(self, index: int, var_type, events: list):
+        self.index = index
+        self.var_type = var_type
+        self._events = events
+
+    def __getitem__(self, idx):
+        return vc.Sym("load", self.index)
+
+    def __setitem__(self, idx, value):
+        self._events.append(("store", self.index, value))
+
+
+class _TraceOp:
+    def __init__(self, events: list):
+        self._events = events
+        self.register = TraceRegister("reg", events)
+        self.io_index = vc.Sym("io_index")
+        self.fft_index = vc.Sym("fft_index")
+        self.fft_size = vc.Sym("fft_size")
+
+    def read_from_buffer(self, buffer, register=None, io_index=None):
+        name = register._name if isinstance(register, TraceRegister) else "reg"
+        self._events.append(("read", buffer.index, name, io_index is None))
+
+    def write_to_buffer(self, buffer, register=None, io_index=None):
+        self._events.append(("write", buffer.index, io_index is None))
+
+
+def read_op():
+    op = getattr(_tls, "read", None)
+    if op is None:
+        raise ValueError("No global read operation is set for the current thread!")
+    return op
+
+
+def write_op():
+    op = getattr(_tls, "write", None)
+    if op is None:
+        raise ValueError("No global write operation is set for the current thread!")
+    return op
+
+
+def new_trace_register(var_type):
+    events = getattr(_tls, "events", None)
+    if events is None:
+        raise ValueError("new_register is only available while a map function is traced")
+    n = getattr(_tls, "nreg", 0)
+    _tls.nreg = n + 1
+    return TraceRegister(f"tmp{n}", events)
+
+
+def _trace(mf, role: str):
+    events: list = []
+    types = mf.input_dtypes()
+    bufs = [_TraceBuffer(i, t, events) for i, t in enumerate(types)]
+    _tls.events, _tls.nreg = events, 0
+    _tls.read = _TraceOp(events) if role in ("input", "kernel") else None
+    _tls.write = _TraceOp(events) if role == "output" else None
+    try:
+        mf.func(*bufs)
+    except NotImplementedError:
+        raise
+    except Exception as e:  # noqa: BLE001
+        raise NotImplementedError(f"{role} map {mf.func.__name__} could not be traced: {e}") from e
+    finally:
+        _tls.events = _tls.read = _tls.write = None
+    return events, types
+
+
+def _has(expr, op, arg=None) -> bool:
+    if not isinstance(expr, vc.Sym):
+        return False
+    if expr.op == op and (arg is None or arg in expr.args):
+        return True
+    return any(_has(a, op, arg) for a in expr.args)
+
+
+def _is_zero(expr) -> bool:
+    if isinstance(expr, (int, float)):
+        return expr == 0
+    return isinstance(expr, vc.Sym) and expr.op == "cast" and _is_zero(expr.args[0])
+
+
+@dataclass
+class IoMap:
+    kind: str  # "complex" or "real"
+    buffer: int  # index among the map's buffers
+    var_type: object
+
+
+@dataclass
+class KernelMap:
+    kind: str  # "conj_mul", "mul", "real_scale" or "identity"
+    buffer: Optional[int]
+    var_type: object
+
+
+def classify_input(mf) -> IoMap:
+    ev, types = _trace(mf, "input")
+    name = mf.func.__name__
+    if len(ev) == 1 and ev[0][0] == "read" and ev[0][2] == "reg" and ev[0][3]:
+        i = ev[0][1]
+        if not types[i].is_complex:
+            raise NotImplementedError(f"input map {name}: read_from_buffer needs a complex buffer")
+        return IoMap("complex", i, types[i])
+    sets = {e[0]: e for e in ev if e[1] == "reg"}
+    if len(ev) == 2 and set(sets) == {"set_real", "set_imag"} and _is_zero(sets["set_imag"][2]):
+        loads = [a for a in range(len(types)) if _has(sets["set_real"][2], "load", a)]
+        if len(loads) == 1 and types[loads[0]] in (dt.float32, dt.float64):
+            return IoMap("real", loads[0], types[loads[0]])
+    raise NotImplementedError(f"input map {name} is not in the supported map menu: {ev}")
+
+
+def classify_output(mf) -> IoMap:
+    ev, types = _trace(mf, "output")
+    name = mf.func.__name__
+    if len(ev) == 1 and ev[0][0] == "write" and ev[0][2]:
+        i = ev[0][1]
+        if not types[i].is_complex:
+            raise NotImplementedError(f"output map {name}: write_to_buffer needs a complex buffer")
+        return IoMap("complex", i, types[i])
+    if len(ev) == 1 and ev[0][0] == "store" and _has(ev[0][2], "reg_real", "reg"):
+        i = ev[0][1]
+        if types[i] in (dt.float32, dt.float64):
+            return IoMap("real", i, types[i])
+    raise NotImplementedError(f"output map {name} is not in the supported map menu: {ev}")
+
+
+def classify_kernel(mf) -> KernelMap:
+    ev, types = _trace(mf, "kernel")
+    name = mf.func.__name__
+    if not ev:
+        return KernelMap("identity", None, None)
+    if len(ev) == 2 and ev[0][0] == "read" and ev[1][0] == "set" and ev[1][1] == "reg":
+        i, reg = ev[0][1], ev[0][2]
+        prod = ev[1][2]
+        if isinstance(prod, vc.Sym) and prod.op == "cmul" and types[i].is_complex:
+            a, b = prod.args
+            if isinstance(a, TraceRegister) and a._name == "reg":
+                if isinstance(b, vc.Sym) and b.op == "conj" and b.args[0].args == (reg,):
+                    return KernelMap("conj_mul", i, types[i])
+                if isinstance(b, TraceRegister) and b._name == reg:
+                    return KernelMap("mul", i, types[i])
+    if len(ev) == 1 and ev[0][0] == "set" and ev[0][1] == "reg":
+        prod = ev[0][2]
+        if isinstance(prod, vc.Sym) and prod.op == "cmul" and _has(prod.args[1], "to_complex"):
+            loads = [a for a in range(len(types)) if _has(prod.args[1], "load", a)]
+            if len(loads) == 1 and types[loads[0]] in (dt.float32, dt.float64):
+                return KernelMap("real_scale", loads[0], types[loads[0]])
+    raise NotImplementedError(f"kernel map {name} is not in the supported map menu: {ev}")

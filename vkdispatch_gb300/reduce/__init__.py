@@ -20,7 +20,7 @@ import numpy as np
 
 from .. import _lib as L
 from .. import codegen as vc
-from .. import dtype as dt
+from .. import dtypes as dt
 from .. import graph as G
 from ..buffer import Buffer
 
