@@ -259,6 +259,7 @@ def run_ours(args):
     extra = cfg1_numbers(vd, torch, flush, args) if rank == 0 and not args.quick else {}
     if rank == 0 and not args.quick:
         extra["cfg3_diff_conv3d_256"] = cfg3_numbers(torch, flush)
+        extra["cfg4_batched_uneven"] = cfg4_numbers(torch)
     cpu = cpu_baseline(images, kernel) if (rank == 0 and not args.quick) else None
 
     if rank == 0:
@@ -440,6 +441,129 @@ def cfg3_numbers(torch, flush, steps=10):
     return out
 
 
+def cfg4_workload(total=2 ** 28, nitems=4096, seed=3):
+    """4096 lengths drawn log-uniformly from the 7-smooth integers in
+    [16, 65536] (nearest in log distance), batch counts b_i = max(1,
+    round(2^28 / (4096 L_i))), the last count trimmed so the points fit 2^28."""
+    smooth = sorted({2 ** a * 3 ** b * 5 ** c * 7 ** d for a in range(17) for b in range(11) for c in range(7)
+                     for d in range(6) if 16 <= 2 ** a * 3 ** b * 5 ** c * 7 ** d <= 65536})
+    logs = np.log(np.array(smooth, dtype=np.float64))
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(np.log(16.0), np.log(65536.0), nitems)
+    lengths = [smooth[int(np.argmin(np.abs(logs - x)))] for x in u]
+    counts = [max(1, int(round(total / (nitems * n)))) for n in lengths]
+    used = sum(n * c for n, c in zip(lengths[:-1], counts[:-1]))
+    counts[-1] = max(1, (total - used) // lengths[-1])
+    return lengths, counts, len(smooth)
+
+
+def cfg4_numbers(torch, reps=10):
+    """Batched uneven lengths: one persistent launch (replayed as a CUDA
+    graph) vs one plain launch per length, issued directly and as a
+    captured graph; algorithmic bytes = read + write of every point once per
+    pass (two passes for lengths above the single-CTA limit)."""
+    import vkdispatch_gb300 as vd
+    from vkdispatch_gb300 import _lib as L
+    from vkdispatch_gb300.batch import BatchPlan, pack_items
+    from vkdispatch_gb300.fft import plan as P
+
+    lengths, counts, nsmooth = cfg4_workload()
+    items, points = pack_items(zip(lengths, counts))
+    g = torch.Generator(device="cuda").manual_seed(3)
+    data = torch.randn(points, dtype=torch.complex64, device="cuda", generator=g)
+    x0 = data.clone()
+    plan = BatchPlan(items)
+    desc = plan.describe()
+    ws = plan.make_workspace()
+    long_points = desc["long_points"]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def timed(fn, n=reps):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(n):
+            ev[0].record()
+            fn()
+            ev[1].record()
+            torch.cuda.synchronize()
+            ts.append(ev[0].elapsed_time(ev[1]))
+        return statistics.median(ts)
+
+    # persistent launch, captured once into a CUDA graph
+    plan(data, ws)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    st = torch.cuda.Stream()
+    st.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(st):
+        with torch.cuda.graph(graph, stream=st):
+            with vd.cuda_graph_capture(torch.cuda.current_stream()):
+                plan(data, ws)
+    torch.cuda.current_stream().wait_stream(st)
+    t_persist = timed(graph.replay)
+    status = plan.status()
+
+    # correctness on a sample of items (one forward pass from the saved input)
+    data.copy_(x0)
+    plan(data, ws)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(0)
+    worst = 0.0
+    for i in rng.choice(len(items), 48, replace=False):
+        off, n, c = items[i]
+        xi = x0[off: off + n * c].reshape(c, n).cpu().numpy().astype(np.complex128)
+        gi = data[off: off + n * c].reshape(c, n).cpu().numpy()
+        ref = np.fft.fft(xi, axis=-1)
+        err = float(np.linalg.norm(gi - ref) / np.linalg.norm(ref))
+        worst = max(worst, err / (5e-7 * max(1.0, np.log2(n))))
+
+    # one plain launch per length (single-CTA plans; single-item batches for the long lengths)
+    launches = []
+    s = lambda: int(torch.cuda.current_stream().cuda_stream)  # noqa: E731
+    for off, n, c in items:
+        try:
+            pl = P.get_plan((c, n), 1, L.VDX_KIND_C2C, False, False, L.VDX_C64, L.VDX_C64)
+            ptr = data.data_ptr() + off * 8
+            launches.append(lambda pl=pl, ptr=ptr: pl.exec(ptr, ptr, None, s()))
+        except ValueError:
+            bp = BatchPlan([(0, n, c)])
+            bws = bp.make_workspace()
+            view = data[off: off + n * c]
+            launches.append(lambda bp=bp, view=view, bws=bws: bp(view, bws))
+
+    def plain():
+        for f in launches:
+            f()
+
+    t_plain = timed(plain, max(3, reps // 3))
+    pgraph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(st):
+        with torch.cuda.graph(pgraph, stream=st):
+            with vd.cuda_graph_capture(torch.cuda.current_stream()):
+                plain()
+    torch.cuda.current_stream().wait_stream(st)
+    t_plain_graph = timed(pgraph.replay)
+    bytes_alg = points * 16 + long_points * 16
+    peak, _ = _load_peaks()
+    del data, x0, ws
+    torch.cuda.empty_cache()
+    return {
+        "items": len(items), "distinct_lengths": len(set(lengths)), "seven_smooth_sizes_in_range": nsmooth,
+        "points": points, "long_points": long_points, "plan": desc,
+        "algorithmic_bytes": bytes_alg,
+        "persistent_graph_ms": round(t_persist, 4),
+        "persistent_GBps": round(bytes_alg / (t_persist * 1e-3) / 1e9, 1),
+        "persistent_frac_of_measured_hbm": round(bytes_alg / (t_persist * 1e-3) / 1e9 / peak, 4),
+        "plain_per_length_ms": round(t_plain, 4),
+        "plain_per_length_graph_ms": round(t_plain_graph, 4),
+        "speedup_vs_plain": round(t_plain / t_persist, 3),
+        "speedup_vs_plain_graph": round(t_plain_graph / t_persist, 3),
+        "wait_status": status,
+        "worst_error_over_bound": round(worst, 4),
+    }
+
+
 def cpu_baseline(images, kernel, budget_s=8.0):
     """The CPU restatement of the reference algorithm (oracle/vdx_ref.c, OpenMP
     over all host threads) on a bounded sample of the workload: as many whole
@@ -523,6 +647,20 @@ def run_profile(args):
     import vkdispatch_gb300 as vd
 
     torch.cuda.set_device(0)
+    if args.profile == "cfg4small":
+        # the batched-uneven distribution at 1/8 scale (2^25 points, 512 items)
+        from vkdispatch_gb300.batch import BatchPlan, pack_items
+
+        lengths, counts, _ = cfg4_workload(total=2 ** 25, nitems=512)
+        items, points = pack_items(zip(lengths, counts))
+        data = torch.randn(points, dtype=torch.complex64, device="cuda")
+        plan = BatchPlan(items)
+        ws = plan.make_workspace()
+        for _ in range(args.steps):
+            plan(data, ws)
+        torch.cuda.synchronize()
+        print("profile case done", plan.describe(), flush=True)
+        return
     if args.profile == "conv2d":
         images, kernel = make_inputs()
         kb = vd.asrfftbuffer(kernel)

@@ -154,6 +154,34 @@ int vdx_fft_plan_ctas(const vdx_plan* plan, int64_t* ctas);
  */
 int vdx_convert(const void* src, int src_type, void* dst, int dst_type, int64_t count, void* stream);
 
+/*
+ * Batched transforms of uneven lengths in one persistent launch.  Each item
+ * is `count` contiguous complex64 transforms of `length` points starting at
+ * element `offset` of the data buffer.  Lengths up to 16384 run as tiles of
+ * whole transforms; longer 13-smooth lengths run as a four-step pair inside
+ * the same launch and need a workspace of vdx_batch_workspace_bytes.  Replaces
+ * one make_fft_shader kernel and launch per (length, batch) in the reference
+ * (vkdispatch/fft/shader_factories.py:11-60, functions.py:104-162).
+ * vdx_batch_exec enqueues two memsets and one launch (capturable in a CUDA
+ * graph); vdx_batch_status reads (synchronously) whether a dependency wait
+ * inside the launch gave up, which leaves the affected items undefined.
+ */
+typedef struct vdx_batch_item {
+  int64_t offset;
+  int32_t length;
+  int32_t count;
+} vdx_batch_item;
+
+typedef struct vdx_batch_plan vdx_batch_plan;
+
+int vdx_batch_plan_create(const vdx_batch_item* items, int nitems, int inverse, int normalize,
+                          vdx_batch_plan** plan);
+int vdx_batch_plan_destroy(vdx_batch_plan* plan);
+int vdx_batch_plan_describe(const vdx_batch_plan* plan, char* buf, size_t n);
+int vdx_batch_workspace_bytes(const vdx_batch_plan* plan, size_t* bytes);
+int vdx_batch_exec(const vdx_batch_plan* plan, void* data, void* workspace, void* stream);
+int vdx_batch_status(const vdx_batch_plan* plan, int* status);
+
 /* reduction operations (vkdispatch/reduce/operations.py:17-66) */
 #define VDX_RED_ADD 0
 #define VDX_RED_MUL 1

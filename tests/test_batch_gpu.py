@@ -1,0 +1,89 @@
+"""GPU tests of the batched uneven-length persistent launch against FP64
+numpy.fft, item by item, including lengths above 16384 (four-step)."""
+
+import numpy as np
+import pytest
+
+from helpers import rel_l2, tol_fp32
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+from vkdispatch_gb300.batch import BatchPlan, pack_items  # noqa: E402
+
+
+def _run(lengths_counts, inverse=False, normalize=True, seed=0):
+    items, total = pack_items(lengths_counts)
+    rng = np.random.default_rng(seed)
+    x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex64)
+    d = torch.from_numpy(x).cuda()
+    plan = BatchPlan(items, inverse=inverse, normalize=normalize)
+    ws = plan.make_workspace()
+    plan(d, ws)
+    torch.cuda.synchronize()
+    assert plan.status() == 0
+    got = d.cpu().numpy()
+    for off, n, c in items:
+        xi = x[off: off + n * c].reshape(c, n).astype(np.complex128)
+        if inverse:
+            ref = np.fft.ifft(xi, axis=-1) * (1.0 if normalize else n)
+        else:
+            ref = np.fft.fft(xi, axis=-1)
+        gi = got[off: off + n * c].reshape(c, n)
+        assert rel_l2(gi, ref) <= 2 * tol_fp32(n), (n, c)
+    return plan
+
+
+def test_mixed_short_lengths():
+    p = _run([(16, 300), (1024, 7), (81, 13), (1000, 3), (16384, 2), (2, 5), (4096, 1), (13 * 16, 9)])
+    d = p.describe()
+    # lengths needing more threads per transform than one CTA has run as four-step pairs
+    assert d["long_items"] <= 3 and d["units"] >= 8
+
+
+def test_long_lengths_four_step():
+    p = _run([(32768, 2), (65536, 1), (20736, 1), (15625, 1), (24576, 2), (64, 100)], seed=1)
+    d = p.describe()
+    assert d["long_items"] >= 4 and d["workspace_bytes"] > 0
+
+
+def test_inverse_and_unnormalised():
+    _run([(512, 9), (65536, 1), (45, 3)], inverse=True, seed=2)
+    _run([(512, 9), (49152, 1)], inverse=True, normalize=False, seed=3)
+
+
+def test_graph_capture_replay():
+    items, total = pack_items([(1024, 16), (32768, 1), (343, 5)])
+    rng = np.random.default_rng(4)
+    x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex64)
+    d = torch.from_numpy(x).cuda()
+    plan = BatchPlan(items)
+    ws = plan.make_workspace()
+    plan(d, ws)  # first call outside capture (plan tables are resident already)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    import vkdispatch_gb300 as vd
+
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            with vd.cuda_graph_capture(torch.cuda.current_stream()):
+                plan(d, ws)
+    torch.cuda.current_stream().wait_stream(s)
+    d.copy_(torch.from_numpy(x))
+    g.replay()
+    g.replay()  # twice: forward of forward
+    torch.cuda.synchronize()
+    got = d.cpu().numpy()
+    for off, n, c in items:
+        xi = x[off: off + n * c].reshape(c, n).astype(np.complex128)
+        ref = np.fft.fft(np.fft.fft(xi, axis=-1), axis=-1)
+        assert rel_l2(got[off: off + n * c].reshape(c, n), ref) <= 4 * tol_fp32(n)
+
+
+def test_bad_items_rejected():
+    with pytest.raises(ValueError):
+        BatchPlan([(0, 17 * 4099, 1)])  # prime factor above 13
+    with pytest.raises(ValueError):
+        BatchPlan([(0, 0, 1)])

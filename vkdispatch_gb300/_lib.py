@@ -47,6 +47,12 @@ EXPORTED = (
     "vdx_fft_exec_ops",
     "vdx_fft_plan_ctas",
     "vdx_convert",
+    "vdx_batch_plan_create",
+    "vdx_batch_plan_destroy",
+    "vdx_batch_plan_describe",
+    "vdx_batch_workspace_bytes",
+    "vdx_batch_exec",
+    "vdx_batch_status",
 )
 VDX_REDUCE_NOALLOC_SCRATCH_BYTES = 1048576
 
@@ -83,6 +89,10 @@ class ExecOps(ctypes.Structure):
     ]
 
 
+class BatchItem(ctypes.Structure):
+    _fields_ = [("offset", ctypes.c_int64), ("length", ctypes.c_int32), ("count", ctypes.c_int32)]
+
+
 class VdxError(RuntimeError):
     """Raised for CUDA-side failures reported by libvdx."""
 
@@ -117,6 +127,18 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.vdx_fft_plan_ctas.argtypes = [vp, ctypes.POINTER(i64)]
     lib.vdx_convert.restype = i32
     lib.vdx_convert.argtypes = [vp, i32, vp, i32, i64, vp]
+    lib.vdx_batch_plan_create.restype = i32
+    lib.vdx_batch_plan_create.argtypes = [ctypes.POINTER(BatchItem), i32, i32, i32, ctypes.POINTER(vp)]
+    lib.vdx_batch_plan_destroy.restype = i32
+    lib.vdx_batch_plan_destroy.argtypes = [vp]
+    lib.vdx_batch_plan_describe.restype = i32
+    lib.vdx_batch_plan_describe.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+    lib.vdx_batch_workspace_bytes.restype = i32
+    lib.vdx_batch_workspace_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
+    lib.vdx_batch_exec.restype = i32
+    lib.vdx_batch_exec.argtypes = [vp, vp, vp, vp]
+    lib.vdx_batch_status.restype = i32
+    lib.vdx_batch_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     lib.vdx_reduce_noalloc.restype = i32
     lib.vdx_reduce_noalloc.argtypes = [i32, i32, i32, vp, i64, i64, vp, vp]
 

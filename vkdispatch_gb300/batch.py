@@ -1,0 +1,83 @@
+"""Batched FFTs of uneven lengths in one persistent launch (libvdx
+vdx_batch_*).  Many transforms of different lengths and batch counts, laid
+out back to back in one complex64 buffer, run in a single kernel launch that
+claims work units from a device queue; capture `BatchPlan.__call__` inside
+``torch.cuda.graph`` (or record it in a CommandGraph) to replay the whole set
+as one graph node group.  The reference runs one generated kernel per length
+(vkdispatch/fft/shader_factories.py:11-60), launched separately.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import json
+from typing import Iterable, Optional, Sequence, Tuple
+
+import torch
+
+from . import _lib as L
+from . import graph as G
+
+
+class BatchPlan:
+    """items: (offset, length, count) per item, offsets in complex elements."""
+
+    def __init__(self, items: Sequence[Tuple[int, int, int]], inverse: bool = False, normalize: bool = True):
+        arr = (L.BatchItem * len(items))()
+        for i, (off, n, c) in enumerate(items):
+            arr[i].offset, arr[i].length, arr[i].count = int(off), int(n), int(c)
+        h = ctypes.c_void_p()
+        L.check(L.lib().vdx_batch_plan_create(arr, len(items), int(bool(inverse)), int(bool(normalize)),
+                                              ctypes.byref(h)), "batch plan")
+        self.handle = h
+        self.items = [tuple(int(v) for v in it) for it in items]
+        self.total_points = max(off + n * c for off, n, c in self.items)
+        ws = ctypes.c_size_t()
+        L.check(L.lib().vdx_batch_workspace_bytes(h, ctypes.byref(ws)), "batch workspace")
+        self.workspace_bytes = int(ws.value)
+
+    def describe(self) -> dict:
+        buf = ctypes.create_string_buffer(1024)
+        L.check(L.lib().vdx_batch_plan_describe(self.handle, buf, len(buf)), "batch describe")
+        return json.loads(buf.value.decode())
+
+    def make_workspace(self) -> Optional[torch.Tensor]:
+        if self.workspace_bytes == 0:
+            return None
+        return torch.empty(self.workspace_bytes // 8, dtype=torch.complex64, device="cuda")
+
+    def __call__(self, data: torch.Tensor, workspace: Optional[torch.Tensor] = None, graph=None) -> None:
+        if data.dtype != torch.complex64 or not data.is_cuda or not data.is_contiguous():
+            raise ValueError("data must be a contiguous complex64 CUDA tensor")
+        if data.numel() < self.total_points:
+            raise ValueError(f"data holds {data.numel()} points, the items need {self.total_points}")
+        if self.workspace_bytes and (workspace is None or workspace.numel() * workspace.element_size()
+                                     < self.workspace_bytes):
+            raise ValueError(f"this batch needs a workspace of {self.workspace_bytes} bytes")
+        dptr = data.data_ptr()
+        wptr = workspace.data_ptr() if workspace is not None else None
+        h = self.handle
+        G.resolve(graph).record(lambda s: L.check(L.lib().vdx_batch_exec(h, dptr, wptr, s), "batch exec"),
+                                (data, workspace))
+
+    def status(self) -> int:
+        """0, or 1 when a dependency wait inside a launch gave up (synchronous)."""
+        st = ctypes.c_int()
+        L.check(L.lib().vdx_batch_status(self.handle, ctypes.byref(st)), "batch status")
+        return int(st.value)
+
+    def __del__(self):
+        try:
+            if self.handle:
+                L.lib().vdx_batch_plan_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def pack_items(lengths_counts: Iterable[Tuple[int, int]]):
+    """Lays (length, count) pairs out back to back: [(offset, length, count)]."""
+    items, off = [], 0
+    for n, c in lengths_counts:
+        items.append((off, int(n), int(c)))
+        off += int(n) * int(c)
+    return items, off

@@ -203,8 +203,8 @@ __device__ __forceinline__ void scatter(const Cx<Re>* v, int nb, int T, int t, i
 // Runs every pass on v, which must already hold the inputs of the first
 // executed pass.  reversed = run radices last-to-first.  Returns with v
 // holding natural-order outputs laid out for the last executed radix.
-template <int MAXE, bool INV, bool STRIDED, class Re>
-__device__ __forceinline__ void run_passes(Cx<Re>* v, const PassPlan& pp, bool reversed, const Place<STRIDED>& pl,
+template <int MAXE, bool INV, class PL, class Re>
+__device__ __forceinline__ void run_passes(Cx<Re>* v, const PassPlan& pp, bool reversed, const PL& pl,
                                            Cx<Re>* sm, const Cx<Re>* tw) {
   const int n = pp.n, P = pp.npass, T = pp.T, t = pl.t;
   int ns = 1;
@@ -286,7 +286,7 @@ struct DynPlan {
   }
   template <bool INV, bool REV, bool STRIDED, class Re>
   __device__ __forceinline__ void run(Cx<Re>* v, const Place<STRIDED>& pl, Cx<Re>* sm, const Cx<Re>* tw) const {
-    run_passes<MAXE, INV, STRIDED, Re>(v, pp, REV, pl, sm, tw);
+    run_passes<MAXE, INV>(v, pp, REV, pl, sm, tw);
   }
 };
 

@@ -64,6 +64,22 @@ int get_table(int dev, int count, int den, bool f64, void** out) {
   return VDX_OK;
 }
 
+int store_of(int t) {
+  switch (t) {
+    case VDX_C64: return ST_C64;
+    case VDX_C32: return ST_C32;
+    case VDX_C128: return ST_C128;
+    case VDX_BF16X2: return ST_BF16;
+    default: return -1;
+  }
+}
+
+size_t store_bytes(int st) { return st == ST_C128 ? 16 : st == ST_C64 ? 8 : 4; }
+
+}  // namespace
+
+namespace vdx {
+
 // ---------------------------------------------------------------------------
 // radix factorisation
 // ---------------------------------------------------------------------------
@@ -123,21 +139,7 @@ bool factor_radices(int n, int maxe, std::vector<int>& radices, std::string& why
   return true;
 }
 
-int store_of(int t) {
-  switch (t) {
-    case VDX_C64: return ST_C64;
-    case VDX_C32: return ST_C32;
-    case VDX_C128: return ST_C128;
-    case VDX_BF16X2: return ST_BF16;
-    default: return -1;
-  }
-}
-
-size_t store_bytes(int st) { return st == ST_C128 ? 16 : st == ST_C64 ? 8 : 4; }
-
-}  // namespace
-
-namespace vdx {
+int get_twiddle_table(int dev, int count, int den, bool f64, void** out) { return get_table(dev, count, den, f64, out); }
 
 int set_error(int code, const char* msg) { return fail(code, msg); }
 
