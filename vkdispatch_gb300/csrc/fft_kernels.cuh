@@ -284,15 +284,14 @@ struct DynPlan {
   __device__ __forceinline__ void last(F&& f) const {
     radix_dispatch(pp.radix[REV ? 0 : pp.npass - 1], f);
   }
-  template <bool INV, bool REV, bool STRIDED, class Re>
-  __device__ __forceinline__ void run(Cx<Re>* v, const Place<STRIDED>& pl, Cx<Re>* sm, const Cx<Re>* tw) const {
+  template <bool INV, bool REV, class PL, class Re>
+  __device__ __forceinline__ void run(Cx<Re>* v, const PL& pl, Cx<Re>* sm, const Cx<Re>* tw) const {
     run_passes<MAXE, INV>(v, pp, REV, pl, sm, tw);
   }
 };
 
-template <int N, int T, int MAXE, bool INV, class Re, bool STRIDED, int NS, int R, int... Rest>
-__device__ __forceinline__ void chain(Cx<Re>* v, const PassPlan& pp, const Place<STRIDED>& pl, Cx<Re>* sm,
-                                      const Cx<Re>* tw) {
+template <int N, int T, int MAXE, bool INV, class Re, class PL, int NS, int R, int... Rest>
+__device__ __forceinline__ void chain(Cx<Re>* v, const PassPlan& pp, const PL& pl, Cx<Re>* sm, const Cx<Re>* tw) {
   butterflies<R, MAXE, INV, Re>(v, N / R, T, pl.t, NS, N, tw);
   if constexpr (sizeof...(Rest) > 0) {
     __syncthreads();
@@ -300,14 +299,14 @@ __device__ __forceinline__ void chain(Cx<Re>* v, const PassPlan& pp, const Place
     __syncthreads();
     constexpr int R2 = RFirst<RList<Rest...>>::value;
     gather<R2, MAXE, Re>(v, N / R2, T, pl.t, [&](int pos) { return sm[pl.sidx(pp, pos)]; });
-    chain<N, T, MAXE, INV, Re, STRIDED, NS * R, Rest...>(v, pp, pl, sm, tw);
+    chain<N, T, MAXE, INV, Re, PL, NS * R, Rest...>(v, pp, pl, sm, tw);
   }
 }
 
-template <int N, int T, int MAXE, bool INV, class Re, bool STRIDED, int... Rs>
-__device__ __forceinline__ void chain_list(RList<Rs...>, Cx<Re>* v, const PassPlan& pp, const Place<STRIDED>& pl,
-                                           Cx<Re>* sm, const Cx<Re>* tw) {
-  chain<N, T, MAXE, INV, Re, STRIDED, 1, Rs...>(v, pp, pl, sm, tw);
+template <int N, int T, int MAXE, bool INV, class Re, class PL, int... Rs>
+__device__ __forceinline__ void chain_list(RList<Rs...>, Cx<Re>* v, const PassPlan& pp, const PL& pl, Cx<Re>* sm,
+                                           const Cx<Re>* tw) {
+  chain<N, T, MAXE, INV, Re, PL, 1, Rs...>(v, pp, pl, sm, tw);
 }
 
 template <int N_, int T_, class L, int MAXE_ = 16>
@@ -328,10 +327,11 @@ struct FixPlan {
   __device__ __forceinline__ void last(F&& f) const {
     f(IC<REV ? RFirst<L>::value : RLast<L>::value>{});
   }
-  template <bool INV, bool REV, bool STRIDED, class Re>
-  __device__ __forceinline__ void run(Cx<Re>* v, const Place<STRIDED>& pl, Cx<Re>* sm, const Cx<Re>* tw) const {
+  // PL: a thread placement (Place<STRIDED> or any type with t and sidx(pp, i))
+  template <bool INV, bool REV, class PL, class Re>
+  __device__ __forceinline__ void run(Cx<Re>* v, const PL& pl, Cx<Re>* sm, const Cx<Re>* tw) const {
     using Order = typename std::conditional<REV, typename RRev<L>::type, L>::type;
-    chain_list<N_, T_, MAXE, INV, Re, STRIDED>(Order{}, v, pp, pl, sm, tw);
+    chain_list<N_, T_, MAXE, INV, Re, PL>(Order{}, v, pp, pl, sm, tw);
   }
 };
 

@@ -178,7 +178,224 @@ struct vdx_plan {
   FftArgs args;
   Launch launch;
   std::vector<int> radices;
+  // four-step long axis (fft_large.cu): N = N1 * N0, processed in chunks of
+  // `chunk_cols` columns x `chunk_outer` outer batches (strided axes) or
+  // `chunk_outer` rows (contiguous axes); `ws` holds one chunk
+  bool fourstep = false;
+  int N1 = 0, N0 = 0;
+  long long inner = 1, outer = 1;
+  long long chunk_cols = 0, chunk_outer = 0;
+  FsArgs fsA{}, fsB{};  // pass plans, twiddles and scale; geometry is set per chunk
+  dim3 blockA, blockB;
+  size_t smemA = 0, smemB = 0;
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  ~vdx_plan() {
+    if (ws) cudaFree(ws);
+  }
 };
+
+namespace {
+
+int sub_pass_plan(int n, int M, PassPlan& pp, std::string& why) {
+  std::vector<int> r;
+  if (!factor_radices(n, 16, r, why)) return VDX_ERR_UNSUPPORTED;
+  std::memset(&pp, 0, sizeof(pp));
+  pp.n = n;
+  pp.npass = (int)r.size();
+  int T = 1;
+  for (int i = 0; i < pp.npass; ++i) {
+    pp.radix[i] = r[i];
+    const int nb = n / r[i];
+    const int per = std::max(1, 16 / r[i]);
+    T = std::max(T, (nb + per - 1) / per);
+  }
+  pp.T = T;
+  pp.M = M;
+  pp.npad = n + 1 + ((n + 1) >> 4) + 1;
+  return VDX_OK;
+}
+
+// Plans an axis as the four-step pair (fft_large.cu).  N0 is the largest
+// divisor of N not above sqrt(N); both short lengths must be 13-smooth (they
+// are, as divisors of a 13-smooth N) and at most 4096.
+int plan_fourstep(vdx_plan* p, long long inner, long long outer, int smem_optin) {
+  const int N = p->N;
+  int N0 = 1;
+  for (int c = 1; (long long)c * c <= N; ++c)
+    if (N % c == 0) N0 = c;
+  const int N1 = N / N0;
+  if (N0 < 8 || N1 > 4096)
+    return fail(VDX_ERR_UNSUPPORTED, "FFT length " + std::to_string(N) + " has no four-step split into two lengths "
+                                     "in [8, 4096]");
+  const size_t sb = store_bytes(p->store);
+  const int mw = int(128 / sb);  // columns per tile: 128-byte row segments
+  std::string why;
+  auto tile_m = [&](int n, long long cols, int T) {
+    int M = (int)std::min<long long>(mw, cols);
+    M = std::max(1, std::min(M, 512 / T));
+    while (M > 1 && size_t(n + 1) * M * 8 > size_t(smem_optin)) M /= 2;
+    return M;
+  };
+  PassPlan ppA, ppB;
+  if (sub_pass_plan(N1, 1, ppA, why) != VDX_OK || sub_pass_plan(N0, 1, ppB, why) != VDX_OK)
+    return fail(VDX_ERR_UNSUPPORTED, why);
+  const bool strided = inner > 1;
+  ppA.M = tile_m(N1, strided ? inner : N0, ppA.T);
+  ppB.M = tile_m(N0, strided ? inner : N1, ppB.T);
+  if (ppA.T * ppA.M > 512 || ppB.T * ppB.M > 512)
+    return fail(VDX_ERR_UNSUPPORTED, "four-step sub-transform needs more than 512 threads");
+
+  // workspace bytes per chunk; 0 = the whole array in one pair of launches.
+  // Chunks small enough to stay in L2 save HBM traffic but each launch is
+  // then a single partial wave, and on GB300 the ramp and drain of those
+  // waves cost more than the traffic saved (16384^2 complex64, strided axis:
+  // 1.39 ms whole-array vs 1.64-2.53 ms for 96-16 MB chunks).
+  long long budget = 0;
+  if (const char* e = std::getenv("VDX_FOURSTEP_WS_MB")) budget = std::atoll(e) << 20;
+  const long long col_bytes = (long long)N * (long long)sb;  // one column (strided) or row (contiguous)
+  if (strided) {
+    long long C = inner;
+    long long O = 1;
+    if (budget > 0) {
+      const long long fit = std::max(1ll, budget / col_bytes);
+      if (fit >= inner) {
+        O = std::max(1ll, std::min(outer, fit / inner));
+      } else {
+        C = std::max<long long>(ppA.M, fit / ppA.M * ppA.M);
+        C = std::min(C, inner);
+      }
+    } else {
+      O = outer;
+    }
+    p->chunk_cols = C;
+    p->chunk_outer = O;
+    p->ws_bytes = size_t(O) * size_t(C) * size_t(col_bytes);
+  } else {
+    long long R = outer;
+    if (budget > 0) R = std::max(1ll, std::min(outer, budget / col_bytes));
+    p->chunk_cols = 1;
+    p->chunk_outer = R;
+    p->ws_bytes = size_t(R) * size_t(col_bytes);
+  }
+  p->fourstep = true;
+  p->N1 = N1;
+  p->N0 = N0;
+  p->inner = inner;
+  p->outer = outer;
+  p->fsA.pp = ppA;
+  p->fsB.pp = ppB;
+  p->blockA = dim3(ppA.T * ppA.M);
+  p->blockB = dim3(ppB.T * ppB.M);
+  p->smemA = size_t(std::max(N1 * ppA.M, (N1 + 1) * ppA.M)) * 8;
+  p->smemB = size_t(N0) * ppB.M * 8;
+  int rc = get_table(p->dev, N1, N1, false, const_cast<void**>(&p->fsA.tw));
+  if (rc == VDX_OK) rc = get_table(p->dev, N0, N0, false, const_cast<void**>(&p->fsB.tw));
+  if (rc == VDX_OK) rc = get_table(p->dev, N, N, false, const_cast<void**>(&p->fsA.twl));
+  if (rc != VDX_OK) return rc;
+  p->fsA.scale = 1.f;
+  p->fsB.scale = float(p->args.scale);
+  cudaError_t e = cudaMalloc(&p->ws, p->ws_bytes);
+  if (e != cudaSuccess) {
+    p->ws = nullptr;
+    return fail(VDX_ERR_NOMEM, std::string("four-step workspace: ") + cudaGetErrorString(e));
+  }
+  return VDX_OK;
+}
+
+cudaError_t exec_fourstep(const vdx_plan* p, const void* in, void* out, cudaStream_t s) {
+  const long long N = p->N, N0 = p->N0, N1 = p->N1, inner = p->inner, outer = p->outer;
+  const size_t sb = store_bytes(p->store);
+  const bool inv = p->op == OP_C2C_INV;
+  const char* src = static_cast<const char*>(in);
+  char* dst = static_cast<char*>(out);
+  Launch la{dim3(1), p->blockA, p->smemA, s}, lb{dim3(1), p->blockB, p->smemB, s};
+  const int MA = p->fsA.pp.M, MB = p->fsB.pp.M;
+  cudaError_t e = cudaSuccess;
+  if (inner > 1) {
+    for (long long o0 = 0; o0 < outer; o0 += p->chunk_outer) {
+      const long long Oc = std::min(p->chunk_outer, outer - o0);
+      for (long long i0 = 0; i0 < inner; i0 += p->chunk_cols) {
+        const long long Cc = std::min(p->chunk_cols, inner - i0);
+        const size_t off = size_t(o0 * N * inner + i0) * sb;
+        FsArgs A = p->fsA;
+        A.in = src + off;
+        A.out = p->ws;
+        A.split = N0;
+        A.in_bs1 = N * inner;
+        A.in_bs2 = inner;
+        A.in_ps = N0 * inner;
+        A.out_bs1 = N * Cc;
+        A.out_bs2 = Cc;
+        A.out_ps = N0 * Cc;
+        A.out_cs = 1;
+        A.ncols = (int)Cc;
+        A.col_tiles = (int)((Cc + MA - 1) / MA);
+        A.tw_from_batch = 1;
+        la.grid = dim3((unsigned)(Oc * N0 * A.col_tiles));
+        e = launch_fourstep_pass(A, la, p->store, inv, 1);
+        if (e != cudaSuccess) return e;
+        FsArgs B = p->fsB;
+        B.in = p->ws;
+        B.out = dst + off;
+        B.split = N1;
+        B.in_bs1 = N * Cc;
+        B.in_bs2 = N0 * Cc;
+        B.in_ps = Cc;
+        B.out_bs1 = N * inner;
+        B.out_bs2 = inner;
+        B.out_ps = N1 * inner;
+        B.out_cs = 1;
+        B.ncols = (int)Cc;
+        B.col_tiles = (int)((Cc + MB - 1) / MB);
+        lb.grid = dim3((unsigned)(Oc * N1 * B.col_tiles));
+        e = launch_fourstep_pass(B, lb, p->store, inv, 0);
+        if (e != cudaSuccess) return e;
+      }
+    }
+    return e;
+  }
+  for (long long r0 = 0; r0 < outer; r0 += p->chunk_outer) {
+    const long long Rr = std::min(p->chunk_outer, outer - r0);
+    const size_t off = size_t(r0 * N) * sb;
+    FsArgs A = p->fsA;
+    A.in = src + off;
+    A.out = p->ws;
+    A.split = 1;
+    A.in_bs1 = N;
+    A.in_bs2 = 0;
+    A.in_ps = N0;
+    A.out_bs1 = N;
+    A.out_bs2 = 0;
+    A.out_ps = 1;
+    A.out_cs = N1;
+    A.ncols = (int)N0;
+    A.col_tiles = (int)((N0 + MA - 1) / MA);
+    A.tw_from_batch = 0;
+    la.grid = dim3((unsigned)(Rr * A.col_tiles));
+    e = launch_fourstep_pass(A, la, p->store, inv, 2);
+    if (e != cudaSuccess) return e;
+    FsArgs B = p->fsB;
+    B.in = p->ws;
+    B.out = dst + off;
+    B.split = 1;
+    B.in_bs1 = N;
+    B.in_bs2 = 0;
+    B.in_ps = N1;
+    B.out_bs1 = N;
+    B.out_bs2 = 0;
+    B.out_ps = N1;
+    B.out_cs = 1;
+    B.ncols = (int)N1;
+    B.col_tiles = (int)((N1 + MB - 1) / MB);
+    lb.grid = dim3((unsigned)(Rr * B.col_tiles));
+    e = launch_fourstep_pass(B, lb, p->store, inv, 0);
+    if (e != cudaSuccess) return e;
+  }
+  return e;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -271,14 +488,38 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
     const int per = std::max(1, maxe / r);
     T = std::max(T, (nb + per - 1) / per);
   }
+  int smem_optin = 0;
+  cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->dev);
+  if (smem_optin <= 0) smem_optin = 48 * 1024;
+
+  // long C2C axes run as a four-step pair of launches: always above the
+  // single-CTA limit, and from VDX_FOURSTEP_MIN points (default 8192) where
+  // one CTA per transform leaves a single CTA per SM
+  {
+    int fs_min = 8192;
+    if (const char* e = std::getenv("VDX_FOURSTEP_MIN")) fs_min = std::atoi(e);
+    const bool fs_allowed = d.kind == VDX_KIND_C2C && !f64 && lo == 0 && hi == N;
+    if (fs_allowed && (T > 1024 || (fs_min > 0 && N >= fs_min))) {
+      p->args.scale = d.normalize ? 1.0 / N : 1.0;
+      p->op = d.inverse ? OP_C2C_INV : OP_C2C_FWD;
+      const int rc = plan_fourstep(p, inner, outer, smem_optin);
+      if (rc == VDX_OK) {
+        *plan = p;
+        return VDX_OK;
+      }
+      if (T > 1024) {
+        delete p;
+        return rc;
+      }
+      if (p->ws) cudaFree(p->ws);
+      p->ws = nullptr;
+      p->fourstep = false;
+    }
+  }
   if (T > 1024) {
     delete p;
     return fail(VDX_ERR_UNSUPPORTED, "FFT length " + std::to_string(n) + " needs more than 1024 threads per transform");
   }
-
-  int smem_optin = 0;
-  cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->dev);
-  if (smem_optin <= 0) smem_optin = 48 * 1024;
   const size_t cbytes = f64 ? 16 : 8;
   const bool strided = inner > 1;
   p->strided = strided;
@@ -402,6 +643,16 @@ int vdx_fft_plan_describe(const vdx_plan* p, char* buf, size_t n) {
   if (!p || !buf || n == 0) return fail(VDX_ERR_INVALID, "plan and buf must be non-NULL");
   std::string r;
   for (size_t i = 0; i < p->radices.size(); ++i) r += (i ? "x" : "") + std::to_string(p->radices[i]);
+  if (p->fourstep) {
+    std::snprintf(buf, n,
+                  "{\"op\": \"%s\", \"N\": %d, \"fourstep\": [%d, %d], \"strided\": %s, "
+                  "\"columns_per_tile\": [%d, %d], \"chunk_columns\": %lld, \"chunk_outer\": %lld, "
+                  "\"workspace_bytes\": %zu, \"block\": [%u, %u], \"smem\": [%zu, %zu]}",
+                  p->op == OP_C2C_INV ? "c2c_inv" : "c2c_fwd", p->N, p->N1, p->N0, p->inner > 1 ? "true" : "false",
+                  p->fsA.pp.M, p->fsB.pp.M, p->chunk_cols, p->chunk_outer, p->ws_bytes, p->blockA.x, p->blockB.x,
+                  p->smemA, p->smemB);
+    return VDX_OK;
+  }
   static const char* ops[] = {"c2c_fwd", "c2c_inv", "conv", "r2c_even", "c2r_even", "r2c_odd", "c2r_odd"};
   std::snprintf(buf, n,
                 "{\"op\": \"%s\", \"N\": %d, \"n\": %d, \"radices\": \"%s\", \"threads_per_transform\": %d, "
@@ -423,6 +674,13 @@ int exec_plan(const vdx_plan* p, const void* in, void* out, const void* kernel, 
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   if (dev != p->dev) return fail(VDX_ERR_INVALID, "plan was created on another device");
+  if (p->fourstep) {
+    if (ops && (ops->in_weight || ops->spec_out || ops->loss_weight))
+      return fail(VDX_ERR_UNSUPPORTED, "fused operations are not available on four-step (long-axis) plans");
+    e = exec_fourstep(p, in, out, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "four-step FFT launch");
+    return VDX_OK;
+  }
   FftArgs a = p->args;
   a.in = in;
   a.out = out;

@@ -48,6 +48,27 @@ cudaError_t launch_dyn_real(const FftArgs& a, const Launch& l, int op);
 
 cudaError_t launch_twiddle(void* tab, int count, int den, bool f64, cudaStream_t s);
 
+// One pass of a four-step long-axis transform (fft_large.cu): tiles of M
+// adjacent columns, one pp.n-point transform per column.  Batch b of the
+// launch starts at (b / split) * bs1 + (b % split) * bs2 elements; point pos
+// of column c is at c + pos * ps on input, and at c * out_cs + pos * out_ps
+// on output.  Grid = batches * col_tiles, block = pp.T * pp.M.
+struct FsArgs {
+  PassPlan pp;
+  const void* in;
+  void* out;
+  const void* tw;   // W_n^k of the short transform
+  const void* twl;  // W_N^k of the whole axis (pass A)
+  long long split;
+  long long in_bs1, in_bs2, out_bs1, out_bs2;
+  long long in_ps, out_ps, out_cs;
+  int ncols, col_tiles;
+  int tw_from_batch;  // pass A: b0 is b % split (strided axes) or the column (contiguous axes)
+  float scale;
+};
+// mode 0: plain store; 1: twiddle, unit-stride columns; 2: twiddle, transposed store (out_ps == 1)
+cudaError_t launch_fourstep_pass(const FsArgs& a, const Launch& l, int store, bool inv, int mode);
+
 // complex64 kernels specialised at compile time for power-of-two n in
 // [16, 16384] (radix-16 passes, n/16 threads per transform)
 template <int N>
