@@ -260,6 +260,7 @@ def run_ours(args):
     if rank == 0 and not args.quick:
         extra["cfg3_diff_conv3d_256"] = cfg3_numbers(torch, flush)
         extra["cfg4_batched_uneven"] = cfg4_numbers(torch)
+        extra["cfg5_mixed_precision_2d_16384"] = cfg5_numbers(torch)
     cpu = cpu_baseline(images, kernel) if (rank == 0 and not args.quick) else None
 
     if rank == 0:
@@ -564,6 +565,142 @@ def cfg4_numbers(torch, reps=10):
     }
 
 
+CFG5_N = 16384
+
+
+def _cfg5_plan(axis, io, flags, **env):
+    """An uncached 16384 x 16384 C2C plan, orthonormal scaling (1/sqrt(N) per
+    axis keeps fp16-stored spectra in range), created under `env`."""
+    from vkdispatch_gb300 import _lib as L
+    from vkdispatch_gb300.fft import plan as P
+
+    d = L.FftDesc()
+    d.ndim = 2
+    d.shape[0] = d.shape[1] = CFG5_N
+    d.axis = axis
+    d.kind = L.VDX_KIND_C2C
+    d.normalize = 2
+    d.io_type = io
+    d.compute_type = L.VDX_C64
+    d.signal_lo, d.signal_hi = -1, -1
+    d.kernel_type = io
+    d.flags = flags
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update({k: str(v) for k, v in env.items()})
+    try:
+        return P.Plan(d)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+def cfg5_numbers(torch, reps=10):
+    """Mixed-precision 2-D C2C FFT of 16384 x 16384 points, re and im N(0,1)
+    (torch generator, seed 4), orthonormal scaling.  Storage complex64
+    (8 B/point), bf16 pairs and fp16 pairs (4 B/point); short transforms on
+    fp32 butterflies or as BF16 tensor-core GEMMs with hi/lo compensation.
+    The plain comparator is the one-CTA-per-transform complex64 path (one
+    launch per axis).  Algorithmic bytes = read + write of the array once per
+    axis; rel_l2 is against scipy.fft.fft2 in FP64 of the stored input.
+    tensor_tflops counts the MMA work the tensor-core passes issue (576 flops
+    per point per pass: DFT-16 and DFT-8 stages, three products each)."""
+    import scipy.fft as sf
+
+    from vkdispatch_gb300 import _lib as L
+
+    N = CFG5_N
+    g = torch.Generator(device="cuda").manual_seed(4)
+    x = torch.view_as_complex(torch.randn((N, N, 2), dtype=torch.float32, device="cuda", generator=g))
+    peak, _ = _load_peaks()
+    pk = ROOT / "MEASURED_PEAKS.json"
+    bf16_peak = json.loads(pk.read_text()).get("bf16_tflops", 1900.0) if pk.exists() else 1900.0
+    tc = L.VDX_FFT_FLAG_TENSOR_CORE
+    variants = [
+        ("c64_plain_single_cta", L.VDX_C64, 0, {"VDX_FOURSTEP_MIN": 0}),
+        ("c64_fp32_butterflies", L.VDX_C64, 0, {}),
+        ("c64_tensor_core", L.VDX_C64, tc, {}),
+        ("bf16_fp32_butterflies", L.VDX_BF16X2, 0, {}),
+        ("bf16_tensor_core", L.VDX_BF16X2, tc, {}),
+        ("fp16_fp32_butterflies", L.VDX_C32, 0, {}),
+        ("fp16_tensor_core", L.VDX_C32, tc, {}),
+    ]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    stream = lambda: int(torch.cuda.current_stream().cuda_stream)  # noqa: E731
+    out, refs = {}, {}
+    for name, io, flags, env in variants:
+        if io == L.VDX_C64:
+            data = x.clone()
+            stored = x  # the input as stored (x itself is never transformed)
+        else:
+            dt = torch.bfloat16 if io == L.VDX_BF16X2 else torch.float16
+            data = torch.view_as_real(x).to(dt).contiguous()
+            stored = torch.view_as_complex(data.float())  # a copy, taken before any transform
+        x0 = data.clone()
+        plans = [_cfg5_plan(ax, io, flags, **env) for ax in (0, 1)]
+        ptr = data.data_ptr()
+
+        def fft2():
+            plans[0].exec(ptr, ptr, None, stream())
+            plans[1].exec(ptr, ptr, None, stream())
+
+        fft2()
+        torch.cuda.synchronize()
+        t2, a0, a1 = [], [], []
+        for _ in range(reps):
+            ev[0].record()
+            plans[0].exec(ptr, ptr, None, stream())
+            ev[1].record()
+            plans[1].exec(ptr, ptr, None, stream())
+            ev[2].record()
+            torch.cuda.synchronize()
+            a0.append(ev[0].elapsed_time(ev[1]))
+            a1.append(ev[1].elapsed_time(ev[2]))
+            t2.append(ev[0].elapsed_time(ev[2]))
+        ms = statistics.median(t2)
+        eb = 8 if io == L.VDX_C64 else 4
+        alg = 2 * 2 * N * N * eb
+        rec = {
+            "fft2_ms": round(ms, 4), "axis0_ms": round(statistics.median(a0), 4),
+            "axis1_ms": round(statistics.median(a1), 4),
+            "algorithmic_bytes": alg, "GBps": round(alg / (ms * 1e-3) / 1e9, 1),
+            "frac_of_measured_hbm": round(alg / (ms * 1e-3) / 1e9 / peak, 4),
+            "plans": [p.describe() for p in plans],
+        }
+        if flags:
+            tf = 4 * 576 * N * N / (ms * 1e-3) / 1e12
+            rec["tensor_tflops"] = round(tf, 1)
+            rec["tensor_frac_of_measured_bf16"] = round(tf / bf16_peak, 4)
+            rec["wait_status"] = max(p.status() for p in plans)
+        # accuracy: one transform of the stored input against FP64
+        data.copy_(x0)
+        fft2()
+        torch.cuda.synchronize()
+        if io not in refs:
+            q = stored.cpu().numpy().astype(np.complex128)
+            refs.clear()
+            refs[io] = torch.from_numpy(sf.fft2(q, norm="ortho", workers=os.cpu_count())).cuda()
+            del q
+        ref = refs[io]
+        got = data if io == L.VDX_C64 else torch.view_as_complex(data.float())
+        rec["rel_l2"] = float(torch.linalg.vector_norm(got.to(torch.complex128) - ref) /
+                              torch.linalg.vector_norm(ref))
+        out[name] = rec
+        del data, x0, stored, got, plans
+        torch.cuda.empty_cache()
+    base = out["c64_plain_single_cta"]["fft2_ms"]
+    four = out["c64_fp32_butterflies"]["fft2_ms"]
+    for rec in out.values():
+        rec["speedup_vs_plain_c64"] = round(base / rec["fft2_ms"], 3)
+        rec["speedup_vs_c64_fp32_fourstep"] = round(four / rec["fft2_ms"], 3)
+    refs.clear()
+    del x
+    torch.cuda.empty_cache()
+    return out
+
+
 def cpu_baseline(images, kernel, budget_s=8.0):
     """The CPU restatement of the reference algorithm (oracle/vdx_ref.c, OpenMP
     over all host threads) on a bounded sample of the workload: as many whole
@@ -660,6 +797,21 @@ def run_profile(args):
             plan(data, ws)
         torch.cuda.synchronize()
         print("profile case done", plan.describe(), flush=True)
+        return
+    if args.profile in ("cfg5small", "cfg5small_fp32"):
+        # four-step passes on 16384 x 4096 bf16 pairs (256 MiB), axis 0; the
+        # tensor-core short transforms or the fp32 butterflies
+        from vkdispatch_gb300 import _lib as L
+        from vkdispatch_gb300.fft import plan as P
+
+        x = torch.randn((16384, 4096, 2), dtype=torch.float32, device="cuda").to(torch.bfloat16)
+        with vd.fft.tensor_core_stages(args.profile == "cfg5small"):
+            p = P.get_plan((16384, 4096), 0, L.VDX_KIND_C2C, False, False, L.VDX_BF16X2, L.VDX_C64)
+        s = int(torch.cuda.current_stream().cuda_stream)
+        for _ in range(args.steps):
+            p.exec(x.data_ptr(), x.data_ptr(), None, s)
+        torch.cuda.synchronize()
+        print("profile case done", p.describe(), flush=True)
         return
     if args.profile == "conv2d":
         images, kernel = make_inputs()

@@ -61,7 +61,9 @@ typedef struct vdx_fft_desc {
   int32_t axis;       /* transformed axis (R2C/C2R: must be ndim-1) */
   int32_t kind;       /* VDX_KIND_* */
   int32_t inverse;    /* C2C: 0 forward (exp(-2 pi i nk/N)), 1 inverse */
-  int32_t normalize;  /* C2C / C2R / CONV: scale the output by 1/N (R2C: ignored) */
+  int32_t normalize;  /* C2C / C2R / CONV: 1 = scale the output by 1/N, 2 = by 1/sqrt(N)
+                         (orthonormal; keeps fp16-stored spectra of long axes in range),
+                         0 = unscaled (R2C: ignored) */
   int32_t io_type;    /* VDX_C64, VDX_C32, VDX_C128 or VDX_BF16X2 */
   int32_t compute_type; /* VDX_C64 (fp32 butterflies) or VDX_C128 (fp64) */
   int64_t signal_lo;  /* input_signal_range: points outside [lo, hi) read as 0; */
@@ -69,8 +71,19 @@ typedef struct vdx_fft_desc {
   int32_t kernel_op;  /* CONV: VDX_KOP_* */
   int32_t kernel_type;/* CONV: storage type of the kernel spectrum */
   int32_t kernel_broadcast; /* CONV: 1 = one kernel spectrum for every outer batch */
-  int32_t reserved;
+  int32_t flags;      /* VDX_FFT_FLAG_* (0 = defaults) */
 } vdx_fft_desc;
+
+/*
+ * desc.flags.  VDX_FFT_FLAG_TENSOR_CORE runs the 128-point short transforms
+ * of a four-step (long-axis, C2C) plan as BF16 tensor-core GEMMs -- a
+ * DFT-16 stage and a DFT-8 stage, each with hi/lo-split three-product
+ * compensation and FP32 accumulation -- instead of fp32 butterflies.
+ * Available for C2C axes of exactly 16384 points (split 128 x 128) with
+ * io_type VDX_C64, VDX_C32 or VDX_BF16X2.  No counterpart in the reference,
+ * whose FFT stages are scalar code (vkdispatch/fft/cooley_tukey.py:55-180).
+ */
+#define VDX_FFT_FLAG_TENSOR_CORE 1
 
 typedef struct vdx_plan vdx_plan;
 
@@ -144,6 +157,14 @@ int vdx_fft_exec_ops(const vdx_plan* plan, const void* in, void* out, const void
 
 /* Number of CTAs one vdx_fft_exec of this plan launches. */
 int vdx_fft_plan_ctas(const vdx_plan* plan, int64_t* ctas);
+
+/*
+ * Device-side status of a plan's bounded waits (synchronising read): 0 = every
+ * wait completed; 1 = a tensor-core MMA completion wait gave up and the
+ * affected tile was not written.  Plans without such waits always report 0.
+ * No counterpart in the reference (its kernels have no waits).
+ */
+int vdx_fft_plan_status(const vdx_plan* plan, int* status);
 
 /*
  * Element-wise conversion of `count` elements between VDX_C64, VDX_C128,

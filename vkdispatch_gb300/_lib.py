@@ -28,6 +28,7 @@ def convert(src_ptr: int, src_type: int, dst_ptr: int, dst_type: int, count: int
 # transform kinds
 VDX_KIND_C2C, VDX_KIND_R2C, VDX_KIND_C2R, VDX_KIND_CONV = range(4)
 VDX_KOP_MUL_CONJ, VDX_KOP_MUL = range(2)
+VDX_FFT_FLAG_TENSOR_CORE = 1
 
 # reductions and maps
 VDX_RED_ADD, VDX_RED_MUL, VDX_RED_MIN, VDX_RED_MAX, VDX_RED_AND, VDX_RED_OR, VDX_RED_XOR = range(7)
@@ -72,7 +73,7 @@ class FftDesc(ctypes.Structure):
         ("kernel_op", ctypes.c_int32),
         ("kernel_type", ctypes.c_int32),
         ("kernel_broadcast", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("flags", ctypes.c_int32),
     ]
 
 
@@ -125,6 +126,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.vdx_fft_exec_ops.argtypes = [vp, vp, vp, vp, ctypes.POINTER(ExecOps), vp]
     lib.vdx_fft_plan_ctas.restype = i32
     lib.vdx_fft_plan_ctas.argtypes = [vp, ctypes.POINTER(i64)]
+    lib.vdx_fft_plan_status.restype = i32
+    lib.vdx_fft_plan_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     lib.vdx_convert.restype = i32
     lib.vdx_convert.argtypes = [vp, i32, vp, i32, i64, vp]
     lib.vdx_batch_plan_create.restype = i32

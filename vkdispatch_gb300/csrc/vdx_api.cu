@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -75,6 +76,12 @@ int store_of(int t) {
 }
 
 size_t store_bytes(int st) { return st == ST_C128 ? 16 : st == ST_C64 ? 8 : 4; }
+
+// desc.normalize: 0 = none, 1 = 1/N, 2 = 1/sqrt(N) (orthonormal)
+double norm_scale(int normalize, int N) {
+  if (normalize == 2) return 1.0 / std::sqrt(double(N));
+  return normalize ? 1.0 / N : 1.0;
+}
 
 }  // namespace
 
@@ -190,8 +197,13 @@ struct vdx_plan {
   size_t smemA = 0, smemB = 0;
   void* ws = nullptr;
   size_t ws_bytes = 0;
+  // tensor-core short transforms (VDX_FFT_FLAG_TENSOR_CORE)
+  bool tensor_core = false;
+  const void* tc_bmat = nullptr;  // DFT operand image, shared per (device, direction)
+  int* d_status = nullptr;        // bounded-wait status word
   ~vdx_plan() {
     if (ws) cudaFree(ws);
+    if (d_status) cudaFree(d_status);
   }
 };
 
@@ -300,6 +312,17 @@ int plan_fourstep(vdx_plan* p, long long inner, long long outer, int smem_optin)
     p->ws = nullptr;
     return fail(VDX_ERR_NOMEM, std::string("four-step workspace: ") + cudaGetErrorString(e));
   }
+  if (p->tensor_core) {
+    // 128-point tiles of 16 (8-byte) or 32 (4-byte) columns, 128 threads
+    if (N1 != 128 || N0 != 128 || ppA.M != ppB.M || (ppA.M != 16 && ppA.M != 32))
+      return fail(VDX_ERR_UNSUPPORTED, "tensor-core stages need 128 x 128 tiles of 16 or 32 columns");
+    e = tc_dft_operands(p->dev, p->op == OP_C2C_INV, &p->tc_bmat);
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->d_status), sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(e, "tensor-core plan set-up");
+    p->blockA = p->blockB = dim3(128);
+    p->smemA = p->smemB = tc_pass_smem(ppA.M);
+  }
   return VDX_OK;
 }
 
@@ -333,7 +356,8 @@ cudaError_t exec_fourstep(const vdx_plan* p, const void* in, void* out, cudaStre
         A.col_tiles = (int)((Cc + MA - 1) / MA);
         A.tw_from_batch = 1;
         la.grid = dim3((unsigned)(Oc * N0 * A.col_tiles));
-        e = launch_fourstep_pass(A, la, p->store, inv, 1);
+        e = p->tensor_core ? launch_fourstep_pass_tc(A, la, p->store, inv, 1, p->tc_bmat, p->d_status)
+                           : launch_fourstep_pass(A, la, p->store, inv, 1);
         if (e != cudaSuccess) return e;
         FsArgs B = p->fsB;
         B.in = p->ws;
@@ -349,7 +373,8 @@ cudaError_t exec_fourstep(const vdx_plan* p, const void* in, void* out, cudaStre
         B.ncols = (int)Cc;
         B.col_tiles = (int)((Cc + MB - 1) / MB);
         lb.grid = dim3((unsigned)(Oc * N1 * B.col_tiles));
-        e = launch_fourstep_pass(B, lb, p->store, inv, 0);
+        e = p->tensor_core ? launch_fourstep_pass_tc(B, lb, p->store, inv, 0, p->tc_bmat, p->d_status)
+                           : launch_fourstep_pass(B, lb, p->store, inv, 0);
         if (e != cudaSuccess) return e;
       }
     }
@@ -373,7 +398,8 @@ cudaError_t exec_fourstep(const vdx_plan* p, const void* in, void* out, cudaStre
     A.col_tiles = (int)((N0 + MA - 1) / MA);
     A.tw_from_batch = 0;
     la.grid = dim3((unsigned)(Rr * A.col_tiles));
-    e = launch_fourstep_pass(A, la, p->store, inv, 2);
+    e = p->tensor_core ? launch_fourstep_pass_tc(A, la, p->store, inv, 2, p->tc_bmat, p->d_status)
+                       : launch_fourstep_pass(A, la, p->store, inv, 2);
     if (e != cudaSuccess) return e;
     FsArgs B = p->fsB;
     B.in = p->ws;
@@ -389,7 +415,8 @@ cudaError_t exec_fourstep(const vdx_plan* p, const void* in, void* out, cudaStre
     B.ncols = (int)N1;
     B.col_tiles = (int)((N1 + MB - 1) / MB);
     lb.grid = dim3((unsigned)(Rr * B.col_tiles));
-    e = launch_fourstep_pass(B, lb, p->store, inv, 0);
+    e = p->tensor_core ? launch_fourstep_pass_tc(B, lb, p->store, inv, 0, p->tc_bmat, p->d_status)
+                       : launch_fourstep_pass(B, lb, p->store, inv, 0);
     if (e != cudaSuccess) return e;
   }
   return e;
@@ -444,6 +471,8 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
       return fail(VDX_ERR_UNSUPPORTED, "VDX_KOP_MUL convolutions need complex64 storage");
   }
   if (real && (st == ST_BF16)) return fail(VDX_ERR_UNSUPPORTED, "real transforms support complex64/complex32/complex128");
+  if (d.flags & ~VDX_FFT_FLAG_TENSOR_CORE) return fail(VDX_ERR_INVALID, "unknown bits in desc.flags");
+  if (d.normalize < 0 || d.normalize > 2) return fail(VDX_ERR_INVALID, "normalize must be 0, 1 or 2");
 
   long long inner = 1, outer = 1;
   for (int i = d.axis + 1; i < d.ndim; ++i) inner *= d.shape[i];
@@ -499,15 +528,22 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
     int fs_min = 8192;
     if (const char* e = std::getenv("VDX_FOURSTEP_MIN")) fs_min = std::atoi(e);
     const bool fs_allowed = d.kind == VDX_KIND_C2C && !f64 && lo == 0 && hi == N;
-    if (fs_allowed && (T > 1024 || (fs_min > 0 && N >= fs_min))) {
-      p->args.scale = d.normalize ? 1.0 / N : 1.0;
+    const bool tcore = (d.flags & VDX_FFT_FLAG_TENSOR_CORE) != 0;
+    if (tcore && !(fs_allowed && N == 16384)) {
+      delete p;
+      return fail(VDX_ERR_UNSUPPORTED, "tensor-core DFT stages need a C2C axis of 16384 points (128 x 128 four-step) "
+                                       "with complex64, complex32 or bf16x2 storage and no signal range");
+    }
+    if (fs_allowed && (tcore || T > 1024 || (fs_min > 0 && N >= fs_min))) {
+      p->tensor_core = tcore;
+      p->args.scale = norm_scale(d.normalize, N);
       p->op = d.inverse ? OP_C2C_INV : OP_C2C_FWD;
       const int rc = plan_fourstep(p, inner, outer, smem_optin);
       if (rc == VDX_OK) {
         *plan = p;
         return VDX_OK;
       }
-      if (T > 1024) {
+      if (T > 1024 || tcore) {
         delete p;
         return rc;
       }
@@ -564,15 +600,14 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
   a.sig_hi = hi;
   a.nreal = N;
 
-  const bool norm = d.normalize != 0;
   switch (d.kind) {
     case VDX_KIND_C2C:
       p->op = d.inverse ? OP_C2C_INV : OP_C2C_FWD;
-      a.scale = norm ? 1.0 / N : 1.0;
+      a.scale = norm_scale(d.normalize, N);
       break;
     case VDX_KIND_CONV:
       p->op = OP_CONV;
-      a.scale = norm ? 1.0 / N : 1.0;
+      a.scale = norm_scale(d.normalize, N);
       break;
     case VDX_KIND_R2C:
       p->op = even_real ? OP_R2C_EVEN : OP_R2C_ODD;
@@ -580,7 +615,7 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
       break;
     default:
       p->op = even_real ? OP_C2R_EVEN : OP_C2R_ODD;
-      a.scale = norm ? 1.0 / N : 1.0;
+      a.scale = norm_scale(d.normalize, N);
       break;
   }
 
@@ -647,10 +682,10 @@ int vdx_fft_plan_describe(const vdx_plan* p, char* buf, size_t n) {
     std::snprintf(buf, n,
                   "{\"op\": \"%s\", \"N\": %d, \"fourstep\": [%d, %d], \"strided\": %s, "
                   "\"columns_per_tile\": [%d, %d], \"chunk_columns\": %lld, \"chunk_outer\": %lld, "
-                  "\"workspace_bytes\": %zu, \"block\": [%u, %u], \"smem\": [%zu, %zu]}",
+                  "\"workspace_bytes\": %zu, \"block\": [%u, %u], \"smem\": [%zu, %zu], \"tensor_core\": %s}",
                   p->op == OP_C2C_INV ? "c2c_inv" : "c2c_fwd", p->N, p->N1, p->N0, p->inner > 1 ? "true" : "false",
                   p->fsA.pp.M, p->fsB.pp.M, p->chunk_cols, p->chunk_outer, p->ws_bytes, p->blockA.x, p->blockB.x,
-                  p->smemA, p->smemB);
+                  p->smemA, p->smemB, p->tensor_core ? "true" : "false");
     return VDX_OK;
   }
   static const char* ops[] = {"c2c_fwd", "c2c_inv", "conv", "r2c_even", "c2r_even", "r2c_odd", "c2r_odd"};
@@ -743,6 +778,15 @@ int vdx_fft_exec_ops(const vdx_plan* p, const void* in, void* out, const void* k
 int vdx_fft_plan_ctas(const vdx_plan* p, int64_t* ctas) {
   if (!p || !ctas) return fail(VDX_ERR_INVALID, "plan and ctas must be non-NULL");
   *ctas = (int64_t)p->launch.grid.x;
+  return VDX_OK;
+}
+
+int vdx_fft_plan_status(const vdx_plan* p, int* status) {
+  if (!p || !status) return fail(VDX_ERR_INVALID, "plan and status must be non-NULL");
+  *status = 0;
+  if (!p->d_status) return VDX_OK;
+  cudaError_t e = cudaMemcpy(status, p->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "plan status read");
   return VDX_OK;
 }
 

@@ -68,6 +68,14 @@ struct FsArgs {
 };
 // mode 0: plain store; 1: twiddle, unit-stride columns; 2: twiddle, transposed store (out_ps == 1)
 cudaError_t launch_fourstep_pass(const FsArgs& a, const Launch& l, int store, bool inv, int mode);
+// The same pass with the 128-point short transforms on the tensor cores
+// (fft_tc.cu); a.pp.n must be 128 and a.pp.M 16 or 32.  bmat = the DFT
+// operand image from tc_dft_operands; *status is set to 1 if an MMA
+// completion wait gives up.
+cudaError_t launch_fourstep_pass_tc(const FsArgs& a, const Launch& l, int store, bool inv, int mode,
+                                    const void* bmat, int* status);
+cudaError_t tc_dft_operands(int dev, bool inv, const void** out);
+size_t tc_pass_smem(int mt);
 
 // complex64 kernels specialised at compile time for power-of-two n in
 // [16, 16384] (radix-16 passes, n/16 threads per transform)

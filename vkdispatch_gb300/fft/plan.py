@@ -3,6 +3,7 @@ kernel factories, vkdispatch/fft/shader_factories.py:11, 107)."""
 
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import json
 import threading
@@ -14,6 +15,25 @@ from .. import _lib as L
 
 _cache: Dict[tuple, "Plan"] = {}
 _mu = threading.Lock()
+_tls = threading.local()
+
+# storage types whose 16384-point C2C axes can run their short transforms on
+# the tensor cores (include/vdx.h: VDX_FFT_FLAG_TENSOR_CORE)
+_TC_IO = (L.VDX_C64, L.VDX_C32, L.VDX_BF16X2)
+
+
+@contextlib.contextmanager
+def tensor_core_stages(enabled: bool = True):
+    """Within the block, C2C transforms along axes of 16384 points run their
+    128-point short transforms as BF16 tensor-core GEMMs with hi/lo-split
+    compensation and FP32 accumulation.  Other plans are unaffected.  The
+    setting is per thread, like the reference's per-thread graph state."""
+    old = getattr(_tls, "tc", False)
+    _tls.tc = bool(enabled)
+    try:
+        yield
+    finally:
+        _tls.tc = old
 
 
 class Plan:
@@ -34,6 +54,12 @@ class Plan:
     def exec_ops(self, in_ptr: int, out_ptr: int, ker_ptr: Optional[int], ops: L.ExecOps, stream: int) -> None:
         L.check(L.lib().vdx_fft_exec_ops(self.handle, in_ptr, out_ptr, ker_ptr, ctypes.byref(ops), stream),
                 "FFT exec")
+
+    def status(self) -> int:
+        """0, or 1 if a bounded device-side wait of this plan gave up."""
+        c = ctypes.c_int()
+        L.check(L.lib().vdx_fft_plan_status(self.handle, ctypes.byref(c)), "FFT plan status")
+        return int(c.value)
 
     def ctas(self) -> int:
         c = ctypes.c_int64()
@@ -60,10 +86,16 @@ def get_plan(
     kernel_op: int = L.VDX_KOP_MUL_CONJ,
     kernel_type: Optional[int] = None,
     kernel_broadcast: bool = False,
+    flags: Optional[int] = None,
 ) -> Plan:
     dev = torch.cuda.current_device()
-    key = (dev, tuple(shape), axis, kind, bool(inverse), bool(normalize), io_type, compute_type, signal_range,
-           kernel_op, kernel_type, bool(kernel_broadcast))
+    if flags is None:
+        flags = 0
+        if (getattr(_tls, "tc", False) and kind == L.VDX_KIND_C2C and int(shape[axis]) == 16384
+                and io_type in _TC_IO and compute_type == L.VDX_C64 and signal_range is None):
+            flags = L.VDX_FFT_FLAG_TENSOR_CORE
+    key = (dev, tuple(shape), axis, kind, bool(inverse), int(normalize), io_type, compute_type, signal_range,
+           kernel_op, kernel_type, bool(kernel_broadcast), int(flags))
     p = _cache.get(key)
     if p is not None:
         return p
@@ -78,7 +110,7 @@ def get_plan(
         d.axis = axis
         d.kind = kind
         d.inverse = int(bool(inverse))
-        d.normalize = int(bool(normalize))
+        d.normalize = int(normalize)  # 0, 1 (1/N) or 2 (1/sqrt(N))
         d.io_type = io_type
         d.compute_type = compute_type
         if signal_range is None:
@@ -88,6 +120,7 @@ def get_plan(
         d.kernel_op = kernel_op
         d.kernel_type = io_type if kernel_type is None else kernel_type
         d.kernel_broadcast = int(bool(kernel_broadcast))
+        d.flags = int(flags)
         p = Plan(d)
         _cache[key] = p
         return p
