@@ -50,6 +50,15 @@ extern "C" {
 #define VDX_KIND_R2C 1  /* real FFT of the last axis, packed RFFT layout */
 #define VDX_KIND_C2R 2  /* inverse real FFT of the last axis, packed RFFT layout */
 #define VDX_KIND_CONV 3 /* fused FFT -> spectrum * op(kernel) -> inverse FFT along one axis */
+/* The whole convolve2DR of real images in one launch (vkdispatch/fft/
+ * functions.py:614-646): rfft of the last axis -> convolve along axis ndim-2
+ * -> irfft, in place on the packed RFFT layout.  shape = the REAL shape
+ * (..., H, W), ndim 2 or 3, axis = ndim-2; complex64 only; in == out.
+ * normalize scales the column inverse by 1/H and the row inverse by 1/W, as
+ * the composed path does.  Plan creation fails with VDX_ERR_UNSUPPORTED for
+ * sizes without a fused kernel (today H = W = 512); callers then run the
+ * three separate transforms. */
+#define VDX_KIND_CONV2D_REAL 4
 
 /* convolution spectrum operations */
 #define VDX_KOP_MUL_CONJ 0 /* spectrum * conj(kernel) (the reference default) */

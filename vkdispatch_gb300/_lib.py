@@ -26,7 +26,7 @@ def convert(src_ptr: int, src_type: int, dst_ptr: int, dst_type: int, count: int
     check(lib().vdx_convert(src_ptr, src_type, dst_ptr, dst_type, count, stream), "convert")
 
 # transform kinds
-VDX_KIND_C2C, VDX_KIND_R2C, VDX_KIND_C2R, VDX_KIND_CONV = range(4)
+VDX_KIND_C2C, VDX_KIND_R2C, VDX_KIND_C2R, VDX_KIND_CONV, VDX_KIND_CONV2D_REAL = range(5)
 VDX_KOP_MUL_CONJ, VDX_KOP_MUL = range(2)
 VDX_FFT_FLAG_TENSOR_CORE = 1
 

@@ -201,6 +201,10 @@ struct vdx_plan {
   bool tensor_core = false;
   const void* tc_bmat = nullptr;  // DFT operand image, shared per (device, direction)
   int* d_status = nullptr;        // bounded-wait status word
+  // one-launch convolve2DR (fft_conv2d.cu)
+  int c2_H = 0, c2_W = 0;
+  long long c2_images = 0;
+  Conv2dArgs c2{};
   ~vdx_plan() {
     if (ws) cudaFree(ws);
     if (d_status) cudaFree(d_status);
@@ -323,6 +327,62 @@ int plan_fourstep(vdx_plan* p, long long inner, long long outer, int smem_optin)
     p->blockA = p->blockB = dim3(128);
     p->smemA = p->smemB = tc_pass_smem(ppA.M);
   }
+  return VDX_OK;
+}
+
+int plan_conv2d_real(const vdx_fft_desc& d, vdx_plan** plan) {
+  if (d.ndim != 2 && d.ndim != 3) return fail(VDX_ERR_INVALID, "the fused 2-D convolution takes 2 or 3 dimensions");
+  if (d.axis != d.ndim - 2) return fail(VDX_ERR_INVALID, "the fused 2-D convolution convolves along axis ndim-2");
+  if (d.io_type != VDX_C64 || d.compute_type != VDX_C64 || d.kernel_type != VDX_C64)
+    return fail(VDX_ERR_UNSUPPORTED, "the fused 2-D convolution runs on complex64 only");
+  if (d.kernel_op != VDX_KOP_MUL_CONJ && d.kernel_op != VDX_KOP_MUL) return fail(VDX_ERR_INVALID, "unknown kernel_op");
+  if (d.normalize != 0 && d.normalize != 1) return fail(VDX_ERR_INVALID, "normalize must be 0 or 1 here");
+  if (d.flags != 0) return fail(VDX_ERR_INVALID, "the fused 2-D convolution takes no flags");
+  if (!(d.signal_lo < 0 && d.signal_hi < 0) && !(d.signal_lo == 0 && d.signal_hi <= 0))
+    return fail(VDX_ERR_UNSUPPORTED, "the fused 2-D convolution takes no signal range");
+  const long long Hl = d.shape[d.ndim - 2], Wl = d.shape[d.ndim - 1];
+  if (Hl > 65536 || Wl > 65536 || !conv2d_real_supported((int)Hl, (int)Wl))
+    return fail(VDX_ERR_UNSUPPORTED, "no fused 2-D convolution kernel for " + std::to_string(Hl) + " x " +
+                                         std::to_string(Wl) + " images (available: 512 x 512)");
+  const int H = (int)Hl, W = (int)Wl;
+  const long long images = d.ndim == 3 ? d.shape[0] : 1;
+  auto* p = new vdx_plan();
+  p->d = d;
+  p->op = OP_CONV2D_REAL;
+  p->store = ST_C64;
+  p->N = W;
+  cudaError_t e = cudaGetDevice(&p->dev);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(e, "cudaGetDevice");
+  }
+  int clusters = 0;
+  e = conv2d_real_max_clusters(H, W, &clusters);
+  if (e != cudaSuccess || clusters < 1) {
+    cudaGetLastError();
+    delete p;
+    return fail(VDX_ERR_UNSUPPORTED, "this device cannot schedule the 8-CTA clusters of the fused 2-D convolution");
+  }
+  p->c2_H = H;
+  p->c2_W = W;
+  p->c2_images = images;
+  Conv2dArgs& c = p->c2;
+  c.ker_bs = d.kernel_broadcast ? 0 : (long long)H * (W / 2 + 1);
+  c.col_scale = d.normalize ? 1.f / float(H) : 1.f;
+  c.row_scale = d.normalize ? 1.f / float(W) : 1.f;
+  void* t = nullptr;
+  int rc = get_table(p->dev, W / 2, W / 2, false, &t);
+  c.tw_row = static_cast<const Cx<float>*>(t);
+  if (rc == VDX_OK) rc = get_table(p->dev, W / 2 + 1, W, false, &t);
+  c.tw2 = static_cast<const Cx<float>*>(t);
+  if (rc == VDX_OK) rc = get_table(p->dev, H, H, false, &t);
+  c.tw_col = static_cast<const Cx<float>*>(t);
+  if (rc != VDX_OK) {
+    delete p;
+    return rc;
+  }
+  p->launch.grid = dim3((unsigned)(images * 8));
+  *plan = p;
   return VDX_OK;
 }
 
@@ -449,7 +509,8 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
   for (int i = 0; i < d.ndim; ++i)
     if (d.shape[i] < 1) return fail(VDX_ERR_INVALID, "every dimension must be >= 1");
   if (d.axis < 0 || d.axis >= d.ndim) return fail(VDX_ERR_INVALID, "axis out of range");
-  if (d.kind < VDX_KIND_C2C || d.kind > VDX_KIND_CONV) return fail(VDX_ERR_INVALID, "unknown transform kind");
+  if (d.kind < VDX_KIND_C2C || d.kind > VDX_KIND_CONV2D_REAL) return fail(VDX_ERR_INVALID, "unknown transform kind");
+  if (d.kind == VDX_KIND_CONV2D_REAL) return plan_conv2d_real(d, plan);
   const bool real = d.kind == VDX_KIND_R2C || d.kind == VDX_KIND_C2R;
   if (real && d.axis != d.ndim - 1)
     return fail(VDX_ERR_INVALID, "R2C/C2R transforms run on the last (contiguous) axis only");
@@ -688,6 +749,13 @@ int vdx_fft_plan_describe(const vdx_plan* p, char* buf, size_t n) {
                   p->smemA, p->smemB, p->tensor_core ? "true" : "false");
     return VDX_OK;
   }
+  if (p->op == OP_CONV2D_REAL) {
+    std::snprintf(buf, n,
+                  "{\"op\": \"conv2d_real\", \"H\": %d, \"W\": %d, \"images\": %lld, \"cluster\": 8, "
+                  "\"kernel_broadcast\": %s}",
+                  p->c2_H, p->c2_W, p->c2_images, p->c2.ker_bs ? "false" : "true");
+    return VDX_OK;
+  }
   static const char* ops[] = {"c2c_fwd", "c2c_inv", "conv", "r2c_even", "c2r_even", "r2c_odd", "c2r_odd"};
   std::snprintf(buf, n,
                 "{\"op\": \"%s\", \"N\": %d, \"n\": %d, \"radices\": \"%s\", \"threads_per_transform\": %d, "
@@ -704,6 +772,22 @@ int exec_plan(const vdx_plan* p, const void* in, void* out, const void* kernel, 
               void* stream) {
   if (!p) return fail(VDX_ERR_INVALID, "plan is NULL");
   if (!in || !out) return fail(VDX_ERR_INVALID, "in and out must be non-NULL device pointers");
+  if (p->op == OP_CONV2D_REAL) {
+    if (in != out) return fail(VDX_ERR_INVALID, "the fused 2-D convolution runs in place (in == out)");
+    if (!kernel) return fail(VDX_ERR_INVALID, "convolution needs a kernel spectrum");
+    if (ops && (ops->in_weight || ops->spec_out || ops->loss_weight))
+      return fail(VDX_ERR_UNSUPPORTED, "fused operations are not available on the fused 2-D convolution");
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev != p->dev) return fail(VDX_ERR_INVALID, "plan was created on another device");
+    Conv2dArgs c = p->c2;
+    c.data = static_cast<Cx<float>*>(out);
+    c.ker = static_cast<const Cx<float>*>(kernel);
+    e = launch_conv2d_real(c, p->c2_H, p->c2_W, p->c2_images, p->d.kernel_op, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "fused 2-D convolution launch");
+    return VDX_OK;
+  }
   if (p->op == OP_CONV && !kernel) return fail(VDX_ERR_INVALID, "convolution needs a kernel spectrum");
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);

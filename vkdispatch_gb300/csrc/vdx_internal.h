@@ -35,7 +35,7 @@ struct MaxE<double> {
 
 // Supported (storage, compute) pairs: complex64/fp32, complex32/fp32,
 // bf16x2/fp32, complex128/fp64.
-enum Op { OP_C2C_FWD, OP_C2C_INV, OP_CONV, OP_R2C_EVEN, OP_C2R_EVEN, OP_R2C_ODD, OP_C2R_ODD };
+enum Op { OP_C2C_FWD, OP_C2C_INV, OP_CONV, OP_R2C_EVEN, OP_C2R_EVEN, OP_R2C_ODD, OP_C2R_ODD, OP_CONV2D_REAL };
 
 template <class S, class Re>
 cudaError_t launch_fft(const FftArgs& a, const Launch& l, int op, bool strided, int kop, int variant);
@@ -76,6 +76,21 @@ cudaError_t launch_fourstep_pass_tc(const FsArgs& a, const Launch& l, int store,
                                     const void* bmat, int* status);
 cudaError_t tc_dft_operands(int dev, bool inv, const void** out);
 size_t tc_pass_smem(int mt);
+
+// One-launch 2-D convolution of real images (fft_conv2d.cu): one image per
+// thread-block cluster, the half spectrum held in the cluster's shared memory.
+struct Conv2dArgs {
+  Cx<float>* data;          // (images, H, W/2 + 1) packed RFFT rows, in place
+  const Cx<float>* ker;     // kernel spectrum, (images or 1, H, W/2 + 1)
+  long long ker_bs;         // elements between images' kernel spectra (0 = broadcast)
+  const Cx<float>* tw_row;  // W_{W/2}^k, k < W/2
+  const Cx<float>* tw2;     // W_W^k, k <= W/2
+  const Cx<float>* tw_col;  // W_H^k, k < H
+  float col_scale, row_scale;
+};
+bool conv2d_real_supported(int H, int W);
+cudaError_t conv2d_real_max_clusters(int H, int W, int* count);
+cudaError_t launch_conv2d_real(const Conv2dArgs& a, int H, int W, long long images, int kop, cudaStream_t s);
 
 // complex64 kernels specialised at compile time for power-of-two n in
 // [16, 16384] (radix-16 passes, n/16 threads per transform)
