@@ -109,7 +109,8 @@ def test_other_sizes_use_the_composed_path():
     assert rel_l2(b.read_real(0), _ref(x, K)) <= 4 * tol_fp32(256)
 
 
-def test_cuda_graph_capture():
+def test_cuda_graph_capture(monkeypatch):
+    monkeypatch.setenv("VDX_FUSED_CONV2D", "1")
     rng = np.random.default_rng(5)
     x = rng.uniform(-1, 1, (2, 512, 512)).astype(np.float32)
     K = np.broadcast_to(_gaussian_spectrum(512, 512), (2, 512, 257)).astype(np.complex64).copy()
