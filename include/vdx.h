@@ -93,6 +93,20 @@ typedef struct vdx_fft_desc {
  * whose FFT stages are scalar code (vkdispatch/fft/cooley_tukey.py:55-180).
  */
 #define VDX_FFT_FLAG_TENSOR_CORE 1
+/*
+ * VDX_FFT_FLAG_AUTOTUNE: plan creation times the candidate plan choices --
+ * threads per CTA (contiguous axes) or columns per tile (strided axes), radix
+ * order, compile-time vs runtime pass lists, and four-step vs one-CTA
+ * transforms for long C2C axes -- on scratch buffers of the same axis length
+ * and stride class (at most VDX_AUTOTUNE_MB, default 256 MB), and keeps the
+ * fastest.  Choices are cached per (device, kind, N, stride class, batch
+ * class, dtype, direction, kernel op/broadcast, signal range); later plans
+ * with the same key reuse them without timing.  The search allocates and
+ * synchronises: create autotuned plans outside stream capture.  The
+ * reference has no autotuner: its planner picks one configuration by a fixed
+ * rule (vkdispatch/fft/config.py:102-190).
+ */
+#define VDX_FFT_FLAG_AUTOTUNE 2
 
 typedef struct vdx_plan vdx_plan;
 
@@ -116,6 +130,13 @@ int vdx_device_count(int* count);
  */
 int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan);
 int vdx_fft_plan_destroy(vdx_plan* plan);
+
+/* Autotune cache (VDX_FFT_FLAG_AUTOTUNE): number of cached choices and of
+ * candidate searches run so far; save to / merge from a text file (one line
+ * per key).  No counterpart in the reference. */
+int vdx_autotune_entries(int64_t* entries, int64_t* searches);
+int vdx_autotune_save(const char* path);
+int vdx_autotune_load(const char* path);
 
 /* Human-readable plan (radices, threads per transform, transforms per CTA). */
 int vdx_fft_plan_describe(const vdx_plan* plan, char* buf, size_t n);

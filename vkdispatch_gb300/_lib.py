@@ -29,6 +29,7 @@ def convert(src_ptr: int, src_type: int, dst_ptr: int, dst_type: int, count: int
 VDX_KIND_C2C, VDX_KIND_R2C, VDX_KIND_C2R, VDX_KIND_CONV, VDX_KIND_CONV2D_REAL = range(5)
 VDX_KOP_MUL_CONJ, VDX_KOP_MUL = range(2)
 VDX_FFT_FLAG_TENSOR_CORE = 1
+VDX_FFT_FLAG_AUTOTUNE = 2
 
 # reductions and maps
 VDX_RED_ADD, VDX_RED_MUL, VDX_RED_MIN, VDX_RED_MAX, VDX_RED_AND, VDX_RED_OR, VDX_RED_XOR = range(7)
@@ -126,6 +127,12 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.vdx_fft_exec_ops.argtypes = [vp, vp, vp, vp, ctypes.POINTER(ExecOps), vp]
     lib.vdx_fft_plan_ctas.restype = i32
     lib.vdx_fft_plan_ctas.argtypes = [vp, ctypes.POINTER(i64)]
+    lib.vdx_autotune_entries.restype = i32
+    lib.vdx_autotune_entries.argtypes = [ctypes.POINTER(i64), ctypes.POINTER(i64)]
+    lib.vdx_autotune_save.restype = i32
+    lib.vdx_autotune_save.argtypes = [ctypes.c_char_p]
+    lib.vdx_autotune_load.restype = i32
+    lib.vdx_autotune_load.argtypes = [ctypes.c_char_p]
     lib.vdx_fft_plan_status.restype = i32
     lib.vdx_fft_plan_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     lib.vdx_convert.restype = i32

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -173,6 +174,16 @@ int check_reduce_args(int op, int map, int in_type, const void* in, long long n,
 
 }  // namespace vdx
 
+namespace vdx {
+// Plan choices the autotuner varies (-1 / 0 = the planner's default).
+struct Tune {
+  int width = -1;     // contiguous axes: threads per CTA; strided axes: columns per tile
+  int order = 0;      // radix passes: 0 = largest radix first, 1 = smallest first
+  int fixed = -1;     // compile-time kernels where available: -1 = yes, 0 = no
+  int fourstep = -1;  // long C2C axes: -1 = from 8192 points (VDX_FOURSTEP_MIN), 0 = only above one CTA, 1 = always
+};
+}  // namespace vdx
+
 struct vdx_plan {
   vdx_fft_desc d;
   int dev;
@@ -201,6 +212,11 @@ struct vdx_plan {
   bool tensor_core = false;
   const void* tc_bmat = nullptr;  // DFT operand image, shared per (device, direction)
   int* d_status = nullptr;        // bounded-wait status word
+  // autotuned choices (VDX_FFT_FLAG_AUTOTUNE)
+  bool tuned = false;
+  Tune tune;
+  float tuned_ms = 0.f;
+  int tuned_candidates = 0;
   // one-launch convolve2DR (fft_conv2d.cu)
   int c2_H = 0, c2_W = 0;
   long long c2_images = 0;
@@ -484,24 +500,9 @@ cudaError_t exec_fourstep(const vdx_plan* p, const void* in, void* out, cudaStre
 
 }  // namespace
 
-extern "C" {
+namespace {
 
-int vdx_version(void) { return 100; }
-
-int vdx_last_error(char* buf, size_t n) {
-  if (!buf || n == 0) return VDX_ERR_INVALID;
-  std::snprintf(buf, n, "%s", g_last_error.c_str());
-  return VDX_OK;
-}
-
-int vdx_device_count(int* count) {
-  if (!count) return fail(VDX_ERR_INVALID, "count is NULL");
-  cudaError_t e = cudaGetDeviceCount(count);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
-  return VDX_OK;
-}
-
-int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
+int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
   if (!desc || !plan) return fail(VDX_ERR_INVALID, "desc and plan must be non-NULL");
   *plan = nullptr;
   const vdx_fft_desc& d = *desc;
@@ -532,7 +533,8 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
       return fail(VDX_ERR_UNSUPPORTED, "VDX_KOP_MUL convolutions need complex64 storage");
   }
   if (real && (st == ST_BF16)) return fail(VDX_ERR_UNSUPPORTED, "real transforms support complex64/complex32/complex128");
-  if (d.flags & ~VDX_FFT_FLAG_TENSOR_CORE) return fail(VDX_ERR_INVALID, "unknown bits in desc.flags");
+  if (d.flags & ~(VDX_FFT_FLAG_TENSOR_CORE | VDX_FFT_FLAG_AUTOTUNE))
+    return fail(VDX_ERR_INVALID, "unknown bits in desc.flags");
   if (d.normalize < 0 || d.normalize > 2) return fail(VDX_ERR_INVALID, "normalize must be 0, 1 or 2");
 
   long long inner = 1, outer = 1;
@@ -570,6 +572,7 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
     delete p;
     return fail(VDX_ERR_UNSUPPORTED, why);
   }
+  if (tune.order == 1) std::reverse(p->radices.begin(), p->radices.end());
 
   // threads per transform: enough that every pass fits in MAXE registers
   int T = 1;
@@ -588,6 +591,8 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
   {
     int fs_min = 8192;
     if (const char* e = std::getenv("VDX_FOURSTEP_MIN")) fs_min = std::atoi(e);
+    if (tune.fourstep == 0) fs_min = 0;  // only where one CTA cannot hold the transform
+    if (tune.fourstep == 1) fs_min = 1;  // wherever the split exists
     const bool fs_allowed = d.kind == VDX_KIND_C2C && !f64 && lo == 0 && hi == N;
     const bool tcore = (d.flags & VDX_FFT_FLAG_TENSOR_CORE) != 0;
     if (tcore && !(fs_allowed && N == 16384)) {
@@ -628,6 +633,7 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
   if (strided) {
     int mcols = 8;
     if (const char* e = std::getenv("VDX_STRIDED_COLUMNS")) mcols = std::max(1, std::min(32, std::atoi(e)));
+    if (tune.width > 0) mcols = std::min(32, tune.width);
     M = (int)std::min<long long>(mcols, inner);
     M = std::max(1, std::min(M, 1024 / T));
     while (M > 1 && need_smem && size_t(n) * M * cbytes > size_t(smem_optin)) M /= 2;
@@ -636,6 +642,7 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
     const long long ntrans = outer;
     int cta_threads = 128;
     if (const char* e = std::getenv("VDX_CTA_THREADS")) cta_threads = std::max(32, std::min(1024, std::atoi(e)));
+    if (tune.width > 0) cta_threads = std::max(32, std::min(1024, tune.width));
     M = std::max(1, cta_threads / T);
     M = (int)std::min<long long>(M, ntrans);
     M = std::max(1, std::min(M, 1024 / T));
@@ -708,7 +715,8 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
   p->launch.block = dim3(T * M);
   p->launch.smem = smem;
   p->fixed = st == ST_C64 && !f64 && has_fixed_c64(n) && p->op != OP_R2C_ODD &&
-             p->op != OP_C2R_ODD && T == n / 16 && std::getenv("VDX_NO_FIXED") == nullptr;
+             p->op != OP_C2R_ODD && T == n / 16 && std::getenv("VDX_NO_FIXED") == nullptr && tune.order == 0 &&
+             tune.fixed != 0;
 
   void* tw = nullptr;
   int rc = get_table(p->dev, n, n, f64, &tw);
@@ -730,6 +738,258 @@ int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
   return VDX_OK;
 }
 
+}  // namespace
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// autotuner: times the candidate plan choices for a (kind, N, stride class,
+// batch class, dtype, direction) on scratch buffers and caches the fastest
+// ---------------------------------------------------------------------------
+using TuneKey = std::array<int, 12>;
+std::mutex g_tune_mu;
+std::map<TuneKey, Tune> g_tuned;
+long long g_tunings = 0;  // candidate searches run (cache misses)
+
+int floor_log2(long long v) {
+  int b = 0;
+  while (b < 40 && (1ll << (b + 1)) <= v) ++b;
+  return b;
+}
+
+TuneKey tune_key(int dev, const vdx_fft_desc& d, long long inner, long long outer) {
+  const int N = (int)d.shape[d.axis];
+  const int ib = inner == 1 ? 0 : 1 + std::min(floor_log2(inner), 20);
+  return TuneKey{dev, d.kind, N, ib, std::min(floor_log2(outer), 24), d.io_type, d.compute_type, d.inverse,
+                 d.kernel_op, d.kernel_broadcast, d.flags & VDX_FFT_FLAG_TENSOR_CORE,
+                 d.signal_lo < 0 && d.signal_hi < 0 ? 0 : 1};
+}
+
+float time_plan(const vdx_plan* p, void* sig, const void* ker, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1) {
+  for (int w = 0; w < 2; ++w)
+    if (vdx_fft_exec(p, sig, sig, ker, s) != VDX_OK) return -1.f;
+  constexpr int reps = 8;
+  cudaEventRecord(e0, s);
+  for (int r = 0; r < reps; ++r) vdx_fft_exec(p, sig, sig, ker, s);
+  cudaEventRecord(e1, s);
+  if (cudaEventSynchronize(e1) != cudaSuccess) return -1.f;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  return ms / reps;
+}
+
+// Autotuned plan creation.  The search runs on a copy of the problem with the
+// same axis length and stride class, shrunk to at most VDX_AUTOTUNE_MB
+// (default 256) MB of data, on a private stream; it allocates and
+// synchronises, so autotuned plans must be created outside stream capture.
+int autotune_plan(const vdx_fft_desc& d0, vdx_plan** plan) {
+  vdx_fft_desc d = d0;
+  d.flags &= ~VDX_FFT_FLAG_AUTOTUNE;
+  if (d.kind == VDX_KIND_CONV2D_REAL) return create_plan(&d, Tune{}, plan);
+  if (d.ndim < 1 || d.ndim > 4 || d.axis < 0 || d.axis >= d.ndim) return create_plan(&d, Tune{}, plan);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  long long inner = 1, outer = 1;
+  for (int i = d.axis + 1; i < d.ndim; ++i) inner *= d.shape[i];
+  for (int i = 0; i < d.axis; ++i) outer *= d.shape[i];
+  const TuneKey key = tune_key(dev, d, inner, outer);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      const int rc = create_plan(&d, it->second, plan);
+      if (rc == VDX_OK) {
+        (*plan)->tuned = true;
+        (*plan)->tune = it->second;
+      }
+      return rc;
+    }
+  }
+  // validate the request (and keep the default choice) before searching
+  vdx_plan* base = nullptr;
+  int rc = create_plan(&d, Tune{}, &base);
+  if (rc != VDX_OK) return rc;
+
+  const long long N = d.shape[d.axis];
+  const bool real = d.kind == VDX_KIND_R2C || d.kind == VDX_KIND_C2R;
+  const long long row = real ? N / 2 + 1 : N;
+  const size_t es = store_bytes(store_of(d.io_type));
+  long long cap = 256ll << 20;
+  if (const char* ev = std::getenv("VDX_AUTOTUNE_MB")) cap = std::max(1ll, (long long)std::atoll(ev)) << 20;
+  long long inner_t = inner;
+  if (inner > 1 && (long long)(row * inner * es) > cap) {
+    inner_t = std::max(1ll, cap / (long long)(row * es));
+    if (inner_t >= 32) inner_t = inner_t / 32 * 32;
+  }
+  const long long outer_t = std::min(outer, std::max(1ll, cap / (long long)(row * inner_t * es)));
+  vdx_fft_desc dt = d;
+  if (inner_t > 1) {
+    dt.ndim = 3;
+    dt.shape[0] = outer_t;
+    dt.shape[1] = N;
+    dt.shape[2] = inner_t;
+  } else {
+    dt.ndim = 2;
+    dt.shape[0] = outer_t;
+    dt.shape[1] = N;
+  }
+  dt.axis = 1;
+  const size_t sig_bytes = size_t(outer_t) * size_t(row) * size_t(inner_t) * es;
+  const size_t ker_bytes = d.kind == VDX_KIND_CONV ? (d.kernel_broadcast ? size_t(row) * size_t(inner_t) * es : sig_bytes)
+                                                    : 0;
+  void* sig = nullptr;
+  void* ker = nullptr;
+  cudaStream_t s = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  e = cudaMalloc(&sig, sig_bytes);
+  if (e == cudaSuccess && ker_bytes) e = cudaMalloc(&ker, ker_bytes);
+  if (e == cudaSuccess) e = cudaMemset(sig, 0, sig_bytes);
+  if (e == cudaSuccess && ker_bytes) e = cudaMemset(ker, 0, ker_bytes);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  Tune best{};
+  float best_ms = -1.f;
+  int tried = 0;
+  if (e == cudaSuccess) {
+    std::vector<int> widths = inner_t > 1 ? std::vector<int>{2, 4, 8, 16, 32}
+                                          : std::vector<int>{64, 128, 256, 512, 1024};
+    const bool fs_opt = d.kind == VDX_KIND_C2C && d.compute_type == VDX_C64 && N >= 2048 &&
+                        (d.signal_lo < 0 && d.signal_hi < 0) && !(d.flags & VDX_FFT_FLAG_TENSOR_CORE);
+    std::vector<Tune> cands;
+    for (int fsv : fs_opt ? std::vector<int>{0, 1} : std::vector<int>{-1})
+      for (int order : {0, 1})
+        for (int fixed : {-1, 0})
+          for (int w : widths) {
+            if (order == 1 && fixed == -1) continue;  // compile-time kernels exist for one order only
+            Tune t;
+            t.width = w;
+            t.order = order;
+            t.fixed = fixed;
+            t.fourstep = fsv;
+            cands.push_back(t);
+          }
+    std::vector<std::string> seen;
+    for (const Tune& t : cands) {
+      vdx_plan* c = nullptr;
+      if (create_plan(&dt, t, &c) != VDX_OK) continue;
+      char sig_desc[1024];
+      vdx_fft_plan_describe(c, sig_desc, sizeof(sig_desc));
+      if (std::find(seen.begin(), seen.end(), std::string(sig_desc)) != seen.end()) {
+        delete c;
+        continue;
+      }
+      seen.emplace_back(sig_desc);
+      const float ms = time_plan(c, sig, ker, s, e0, e1);
+      ++tried;
+      delete c;
+      if (ms > 0.f && (best_ms < 0.f || ms < best_ms)) {
+        best_ms = ms;
+        best = t;
+      }
+    }
+  }
+  if (e1) cudaEventDestroy(e1);
+  if (e0) cudaEventDestroy(e0);
+  if (s) cudaStreamDestroy(s);
+  if (ker) cudaFree(ker);
+  if (sig) cudaFree(sig);
+  cudaGetLastError();
+  if (best_ms < 0.f) {  // nothing could be timed: keep the default choice
+    *plan = base;
+    return VDX_OK;
+  }
+  delete base;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tuned[key] = best;
+    ++g_tunings;
+  }
+  rc = create_plan(&d, best, plan);
+  if (rc == VDX_OK) {
+    (*plan)->tuned = true;
+    (*plan)->tune = best;
+    (*plan)->tuned_ms = best_ms;
+    (*plan)->tuned_candidates = tried;
+  }
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vdx_version(void) { return 100; }
+
+int vdx_last_error(char* buf, size_t n) {
+  if (!buf || n == 0) return VDX_ERR_INVALID;
+  std::snprintf(buf, n, "%s", g_last_error.c_str());
+  return VDX_OK;
+}
+
+int vdx_device_count(int* count) {
+  if (!count) return fail(VDX_ERR_INVALID, "count is NULL");
+  cudaError_t e = cudaGetDeviceCount(count);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+  return VDX_OK;
+}
+
+int vdx_fft_plan_create(const vdx_fft_desc* desc, vdx_plan** plan) {
+  if (!desc || !plan) return fail(VDX_ERR_INVALID, "desc and plan must be non-NULL");
+  *plan = nullptr;
+  if (desc->flags & VDX_FFT_FLAG_AUTOTUNE) return autotune_plan(*desc, plan);
+  return create_plan(desc, Tune{}, plan);
+}
+
+int vdx_autotune_entries(int64_t* entries, int64_t* searches) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  if (entries) *entries = (int64_t)g_tuned.size();
+  if (searches) *searches = (int64_t)g_tunings;
+  return VDX_OK;
+}
+
+int vdx_autotune_save(const char* path) {
+  if (!path) return fail(VDX_ERR_INVALID, "path is NULL");
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  FILE* f = std::fopen(path, "w");
+  if (!f) return fail(VDX_ERR_INVALID, std::string("cannot write ") + path);
+  std::fprintf(f, "# libvdx autotune cache: 12 key fields, then width order fixed fourstep\n");
+  for (const auto& kv : g_tuned) {
+    for (int v : kv.first) std::fprintf(f, "%d ", v);
+    std::fprintf(f, "%d %d %d %d\n", kv.second.width, kv.second.order, kv.second.fixed, kv.second.fourstep);
+  }
+  std::fclose(f);
+  return VDX_OK;
+}
+
+int vdx_autotune_load(const char* path) {
+  if (!path) return fail(VDX_ERR_INVALID, "path is NULL");
+  FILE* f = std::fopen(path, "r");
+  if (!f) return fail(VDX_ERR_INVALID, std::string("cannot read ") + path);
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  char line[512];
+  int loaded = 0;
+  while (std::fgets(line, sizeof(line), f)) {
+    if (line[0] == '#') continue;
+    TuneKey k{};
+    Tune t;
+    int v[16];
+    int cnt = std::sscanf(line, "%d %d %d %d %d %d %d %d %d %d %d %d %d %d %d %d", &v[0], &v[1], &v[2], &v[3], &v[4],
+                          &v[5], &v[6], &v[7], &v[8], &v[9], &v[10], &v[11], &v[12], &v[13], &v[14], &v[15]);
+    if (cnt != 16) continue;
+    for (int i = 0; i < 12; ++i) k[i] = v[i];
+    t.width = v[12];
+    t.order = v[13];
+    t.fixed = v[14];
+    t.fourstep = v[15];
+    g_tuned[k] = t;
+    ++loaded;
+  }
+  std::fclose(f);
+  return loaded >= 0 ? VDX_OK : VDX_ERR_INVALID;
+}
+
 int vdx_fft_plan_destroy(vdx_plan* plan) {
   delete plan;
   return VDX_OK;
@@ -743,10 +1003,12 @@ int vdx_fft_plan_describe(const vdx_plan* p, char* buf, size_t n) {
     std::snprintf(buf, n,
                   "{\"op\": \"%s\", \"N\": %d, \"fourstep\": [%d, %d], \"strided\": %s, "
                   "\"columns_per_tile\": [%d, %d], \"chunk_columns\": %lld, \"chunk_outer\": %lld, "
-                  "\"workspace_bytes\": %zu, \"block\": [%u, %u], \"smem\": [%zu, %zu], \"tensor_core\": %s}",
+                  "\"workspace_bytes\": %zu, \"block\": [%u, %u], \"smem\": [%zu, %zu], \"tensor_core\": %s, "
+                  "\"autotuned\": %s, \"tune_candidates\": %d}",
                   p->op == OP_C2C_INV ? "c2c_inv" : "c2c_fwd", p->N, p->N1, p->N0, p->inner > 1 ? "true" : "false",
                   p->fsA.pp.M, p->fsB.pp.M, p->chunk_cols, p->chunk_outer, p->ws_bytes, p->blockA.x, p->blockB.x,
-                  p->smemA, p->smemB, p->tensor_core ? "true" : "false");
+                  p->smemA, p->smemB, p->tensor_core ? "true" : "false", p->tuned ? "true" : "false",
+                  p->tuned_candidates);
     return VDX_OK;
   }
   if (p->op == OP_CONV2D_REAL) {
@@ -760,9 +1022,11 @@ int vdx_fft_plan_describe(const vdx_plan* p, char* buf, size_t n) {
   std::snprintf(buf, n,
                 "{\"op\": \"%s\", \"N\": %d, \"n\": %d, \"radices\": \"%s\", \"threads_per_transform\": %d, "
                 "\"transforms_per_cta\": %d, \"strided\": %s, \"fixed\": %s, \"grid\": %u, \"block\": %u, "
-                "\"smem\": %zu}",
+                "\"smem\": %zu, \"autotuned\": %s, \"tune\": [%d, %d, %d, %d], \"tune_candidates\": %d}",
                 ops[p->op], p->N, p->args.pp.n, r.c_str(), p->args.pp.T, p->args.pp.M, p->strided ? "true" : "false",
-                p->fixed ? "true" : "false", p->launch.grid.x, p->launch.block.x, p->launch.smem);
+                p->fixed ? "true" : "false", p->launch.grid.x, p->launch.block.x, p->launch.smem,
+                p->tuned ? "true" : "false", p->tune.width, p->tune.order, p->tune.fixed, p->tune.fourstep,
+                p->tuned_candidates);
   return VDX_OK;
 }
 

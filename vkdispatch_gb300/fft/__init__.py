@@ -22,4 +22,4 @@ from .functions import (  # noqa: F401
     transpose,
 )
 from .maps import read_op, write_op  # noqa: F401
-from .plan import get_plan, tensor_core_stages  # noqa: F401
+from .plan import autotune, autotune_load, autotune_save, autotune_stats, get_plan, tensor_core_stages  # noqa: F401

@@ -23,6 +23,36 @@ _TC_IO = (L.VDX_C64, L.VDX_C32, L.VDX_BF16X2)
 
 
 @contextlib.contextmanager
+def autotune(enabled: bool = True):
+    """Within the block, new plans time their candidate choices (threads per
+    CTA or columns per tile, radix order, compile-time kernels, four-step
+    split) on scratch buffers and keep the fastest, cached per (kind, N,
+    stride class, batch class, dtype, direction).  Create such plans outside
+    CUDA-graph capture: the search allocates and synchronises.  Per thread."""
+    old = getattr(_tls, "tune", False)
+    _tls.tune = bool(enabled)
+    try:
+        yield
+    finally:
+        _tls.tune = old
+
+
+def autotune_stats() -> Tuple[int, int]:
+    """(cached choices, candidate searches run) of this process."""
+    a, b = ctypes.c_int64(), ctypes.c_int64()
+    L.check(L.lib().vdx_autotune_entries(ctypes.byref(a), ctypes.byref(b)), "autotune stats")
+    return int(a.value), int(b.value)
+
+
+def autotune_save(path: str) -> None:
+    L.check(L.lib().vdx_autotune_save(str(path).encode()), "autotune save")
+
+
+def autotune_load(path: str) -> None:
+    L.check(L.lib().vdx_autotune_load(str(path).encode()), "autotune load")
+
+
+@contextlib.contextmanager
 def tensor_core_stages(enabled: bool = True):
     """Within the block, C2C transforms along axes of 16384 points run their
     128-point short transforms as BF16 tensor-core GEMMs with hi/lo-split
@@ -94,6 +124,8 @@ def get_plan(
         if (getattr(_tls, "tc", False) and kind == L.VDX_KIND_C2C and int(shape[axis]) == 16384
                 and io_type in _TC_IO and compute_type == L.VDX_C64 and signal_range is None):
             flags = L.VDX_FFT_FLAG_TENSOR_CORE
+        if getattr(_tls, "tune", False):
+            flags |= L.VDX_FFT_FLAG_AUTOTUNE
     key = (dev, tuple(shape), axis, kind, bool(inverse), int(normalize), io_type, compute_type, signal_range,
            kernel_op, kernel_type, bool(kernel_broadcast), int(flags))
     p = _cache.get(key)
