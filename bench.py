@@ -359,6 +359,31 @@ def cfg1_numbers(vd, torch, flush, args):
     out["cfg1_256x1024_fwd_inv_magsum"] = {"ms_per_step": round(ms, 5),
                                            "GBps": round(10485760 / (ms * 1e-3) / 1e9, 1),
                                            "magnitude_sum": s, "launches_per_step": 4}
+    # the same step captured once in a CUDA graph (vd.cuda_graph_capture) and
+    # replayed: the device time without the per-launch host overhead
+    try:
+        g = torch.cuda.CUDAGraph()
+        st = torch.cuda.Stream()
+        st.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(st):
+            with torch.cuda.graph(g, stream=st):
+                with vd.cuda_graph_capture(torch.cuda.current_stream()):
+                    rg = small_step()
+        torch.cuda.current_stream().wait_stream(st)
+        for _ in range(5):
+            g.replay()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(n):
+            g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        gms = e0.elapsed_time(e1) / n
+        out["cfg1_256x1024_fwd_inv_magsum"].update({
+            "graph_ms_per_step": round(gms, 5), "graph_GBps": round(10485760 / (gms * 1e-3) / 1e9, 1),
+            "graph_magnitude_sum": float(rg.read(0)[0])})
+    except Exception as exc:  # report, do not fail the benchmark
+        out["cfg1_256x1024_fwd_inv_magsum"]["graph_error"] = str(exc)[:200]
 
     big = torch.empty((262144, 1024), dtype=torch.complex64, device="cuda")
     big.normal_()

@@ -170,3 +170,32 @@ def test_map_classification_menu():
     assert M.classify_kernel(vd.map(nothing)).kind == "identity"
     with pytest.raises(ValueError):
         vd.fft.read_op()  # only valid while a map function is traced
+
+
+def test_multi_kernel_map_strides_are_recognised():
+    """Kernel and output maps of a multi-kernel convolution index their buffers
+    with io_index + mapped_kernel_index() * C (either operand order); other
+    index expressions are refused."""
+    import vkdispatch_gb300 as vd
+    import vkdispatch_gb300.codegen as vc
+    from vkdispatch_gb300.fft import maps as M
+
+    def kmap(kernels: vc.Buffer[vd.complex64]):
+        op = vd.fft.read_op()
+        kv = vc.new_register(vd.complex64)
+        op.read_from_buffer(kernels, register=kv, io_index=vd.fft.mapped_kernel_index() * 96 + op.io_index)
+        op.register[:] = vc.mult_complex(op.register, kv.conjugate())
+
+    def omap(out: vc.Buffer[vd.complex64]):
+        op = vd.fft.write_op()
+        op.write_to_buffer(out, io_index=op.io_index + 40 * vd.fft.mapped_kernel_index())
+
+    def bad(out: vc.Buffer[vd.complex64]):
+        op = vd.fft.write_op()
+        op.write_to_buffer(out, io_index=op.io_index * 2)
+
+    assert M.classify_kernel(vd.map(kmap)).stride == 96
+    assert M.classify_output(vd.map(omap)).stride == 40
+    assert vd.fft.mapped_kernel_index() is None
+    with pytest.raises(NotImplementedError):
+        M.classify_output(vd.map(bad))

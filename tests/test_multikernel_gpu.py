@@ -1,0 +1,94 @@
+"""Multi-kernel convolution (kernel_num > 1, vkdispatch/fft/shader_factories.py:
+166-193): one signal against a bank of kernel spectra, the kernel map and the
+output map indexing their buffers with ``io_index + mapped_kernel_index() * C``.
+Checked against FP64 numpy per kernel, within the fused convolution's
+tolerance (forward + inverse pass)."""
+
+import numpy as np
+import pytest
+
+from helpers import crandn, rel_l2, tol_fp32
+
+pytestmark = pytest.mark.gpu
+
+vd = pytest.importorskip("vkdispatch_gb300")
+import vkdispatch_gb300.codegen as vc  # noqa: E402
+
+
+def _maps(slab, conj=True):
+    def kernel_map(kernels: vc.Buffer[vd.complex64]):
+        op = vd.fft.read_op()
+        kv = vc.new_register(vd.complex64)
+        op.read_from_buffer(kernels, register=kv, io_index=op.io_index + vd.fft.mapped_kernel_index() * slab)
+        op.register[:] = vc.mult_complex(op.register, kv.conjugate() if conj else kv)
+
+    def output_map(out: vc.Buffer[vd.complex64]):
+        op = vd.fft.write_op()
+        op.write_to_buffer(out, io_index=op.io_index + slab * vd.fft.mapped_kernel_index())
+
+    return vd.map(kernel_map), vd.map(output_map)
+
+
+@pytest.mark.parametrize("axis", [1, 0])
+def test_kernel_bank_into_output_slices(axis):
+    rng = np.random.default_rng(12 + axis)
+    B, N, K = 6, 256, 5
+    shape = (B, N) if axis == 1 else (N, B)
+    x = crandn(rng, shape)
+    bank = crandn(rng, (K,) + shape) * 0.1
+    slab = B * N
+    km, om = _maps(slab)
+    sig, kb = vd.asbuffer(x), vd.asbuffer(bank.reshape((K * shape[0],) + shape[1:]))
+    out = vd.Buffer((K * shape[0],) + shape[1:], vd.complex64)
+    vd.fft.convolve(out, sig, kb, kernel_map=km, output_map=om, kernel_num=K, buffer_shape=shape, axis=axis)
+    got = out.read(0).reshape((K,) + shape)
+    s = np.fft.fft(x.astype(np.complex128), axis=axis)
+    for k in range(K):
+        ref = np.fft.ifft(s * np.conj(bank[k]), axis=axis)
+        assert rel_l2(got[k], ref) <= 2 * tol_fp32(N)
+    assert rel_l2(sig.read(0), x) == 0.0  # the signal is not modified
+
+
+def test_in_place_bank_reads_the_original_signal():
+    # the output map writes slice k over a buffer whose slice 0 is the signal:
+    # every kernel must still see the original signal
+    rng = np.random.default_rng(21)
+    B, N, K = 4, 128, 3
+    x = crandn(rng, (B, N))
+    bank = crandn(rng, (K, B, N)) * 0.1
+    slab = B * N
+    km, om = _maps(slab, conj=False)
+    buf = vd.Buffer((K * B, N), vd.complex64)
+    init = np.zeros((K * B, N), np.complex64)
+    init[:B] = x
+    buf.write(init)
+    kb = vd.asbuffer(bank.reshape(K * B, N))
+    vd.fft.convolve(buf, buf, kb, kernel_map=km, output_map=om, kernel_num=K, buffer_shape=(B, N), axis=1)
+    got = buf.read(0).reshape(K, B, N)
+    s = np.fft.fft(x.astype(np.complex128), axis=1)
+    for k in range(K):
+        assert rel_l2(got[k], np.fft.ifft(s * bank[k], axis=1)) <= 2 * tol_fp32(N)
+
+
+def test_default_maps_repeat_the_single_convolution():
+    # without maps every kernel index reads the same kernel and writes the same
+    # output, as in the reference: the result is the single convolution
+    rng = np.random.default_rng(22)
+    x = crandn(rng, (3, 64))
+    k = crandn(rng, (3, 64))
+    a, b = vd.asbuffer(x), vd.asbuffer(x)
+    vd.fft.convolve(a, vd.asbuffer(k), kernel_num=3)
+    vd.fft.convolve(b, vd.asbuffer(k))
+    assert rel_l2(a.read(0), b.read(0)) <= 2 * tol_fp32(64)
+
+
+def test_unrecognised_index_expression_is_refused():
+    def bad_map(kernels: vc.Buffer[vd.complex64]):
+        op = vd.fft.read_op()
+        kv = vc.new_register(vd.complex64)
+        op.read_from_buffer(kernels, register=kv, io_index=op.io_index * 2)
+        op.register[:] = vc.mult_complex(op.register, kv.conjugate())
+
+    b = vd.Buffer((2, 32), vd.complex64)
+    with pytest.raises(NotImplementedError):
+        vd.fft.convolve(b, b, vd.Buffer((4, 32), vd.complex64), kernel_map=vd.map(bad_map), kernel_num=2)

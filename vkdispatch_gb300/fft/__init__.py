@@ -21,5 +21,5 @@ from .functions import (  # noqa: F401
     rfft3,
     transpose,
 )
-from .maps import read_op, write_op  # noqa: F401
+from .maps import mapped_kernel_index, read_op, write_op  # noqa: F401
 from .plan import autotune, autotune_load, autotune_save, autotune_stats, get_plan, tensor_core_stages  # noqa: F401

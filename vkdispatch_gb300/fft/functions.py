@@ -392,8 +392,12 @@ def convolve(
         raise ValueError("At least one buffer must be provided")
     if kernel_map is None and len(buffers) < 2:
         raise ValueError("convolve() requires at least an output buffer and kernel buffer")
-    if kernel_num != 1:
-        raise NotImplementedError("kernel_num > 1 is not supported by this build")
+    if kernel_num < 1:
+        raise ValueError("kernel_num must be >= 1")
+    if kernel_num > 1:
+        _convolve_multi(buffers, kernel_map, kernel_num, buffer_shape, graph, axis, normalize, kernel_inner_only,
+                        input_map, output_map, compute_type, input_signal_range)
+        return
     if input_map is not None or output_map is not None or kernel_map is not None:
         _convolve_mapped(buffers, kernel_map, buffer_shape, graph, axis, normalize, kernel_inner_only, input_map,
                          output_map, compute_type, input_signal_range)
@@ -502,6 +506,79 @@ def _convolve_mapped(buffers, kernel_map, buffer_shape, graph, axis, normalize, 
         raise ValueError(f"kernel buffer of {kbuf.size} elements is smaller than the signal ({total})")
     _staged(lambda c: P.get_plan(shape, ax, L.VDX_KIND_CONV, False, normalize, c, c, sr, kop, c, broadcast),
             out_buf, out_kind, in_buf, in_kind, shape, compute, graph, ker=kptr, keep=keep, pre=pre)
+
+
+def _convolve_multi(buffers, kernel_map, kernel_num, buffer_shape, graph, axis, normalize, kernel_inner_only,
+                    input_map, output_map, compute_type, input_signal_range):
+    """kernel_num convolutions of one signal (vkdispatch/fft/shader_factories.py:
+    166-193): for kernel k the kernel map reads, and the output map writes,
+    ``io_index + mapped_kernel_index() * C`` -- C * k elements along their
+    buffers (C = 0 when the map does not use the index).  One fused
+    convolution launch per kernel; the signal is read from a copy when an
+    output slice overlaps it, so every kernel sees the original signal, as in
+    the reference's single pass over the input."""
+    import torch
+
+    from . import maps as M
+
+    outs, ins, kers = _split_buffers(buffers, input_map, output_map, kernel_map, conv=True)
+    if output_map is not None:
+        om = M.classify_output(output_map)
+        if om.kind != "complex":
+            raise NotImplementedError("multi-kernel convolutions write complex outputs")
+        out_buf, ostride = outs[om.buffer], om.stride
+    else:
+        out_buf, ostride = outs[0], 0
+    if input_map is not None:
+        im = M.classify_input(input_map)
+        if im.kind != "complex":
+            raise NotImplementedError("multi-kernel convolutions read complex inputs")
+        in_buf = ins[im.buffer]
+    else:
+        in_buf = ins[0] if ins else out_buf
+    if kernel_map is not None:
+        km = M.classify_kernel(kernel_map)
+        if km.kind not in ("conj_mul", "mul"):
+            raise NotImplementedError(f"kernel map {kernel_map.func.__name__}: multi-kernel convolutions take a "
+                                      "(conjugate) product with a kernel buffer")
+        kbuf, kstride, kind = kers[km.buffer], km.stride, km.kind
+    else:
+        kbuf, kstride, kind = kers[0], 0, "conj_mul"
+    vt = out_buf.var_type
+    if in_buf.var_type != vt or kbuf.var_type != vt or vt not in (dt.complex64, dt.complex128):
+        raise NotImplementedError("multi-kernel convolutions need complex64 (or complex128) signal, kernel and output")
+    compute = resolve_compute_precision([vt], compute_type)
+    code = vt.vdx_code
+    if _compute_code(vt, compute) != code:
+        raise NotImplementedError("multi-kernel convolutions compute in their storage precision")
+    shape = tuple(int(x) for x in (buffer_shape if buffer_shape is not None else in_buf.shape))
+    ax = _norm_axis(axis, len(shape))
+    total, slab = int(np.prod(shape)), int(np.prod(shape[ax:]))
+    broadcast = bool(kernel_inner_only) or (kbuf.size - (kernel_num - 1) * kstride < total)
+    need_k = (kernel_num - 1) * kstride + (slab if broadcast else total)
+    if kbuf.size < need_k:
+        raise ValueError(f"kernel buffer of {kbuf.size} elements is smaller than the {need_k} the kernels need")
+    if out_buf.size < (kernel_num - 1) * ostride + total or in_buf.size < total:
+        raise ValueError("output buffer too small for kernel_num slices of the signal shape")
+    kop = L.VDX_KOP_MUL_CONJ if kind == "conj_mul" else L.VDX_KOP_MUL
+    plan = P.get_plan(shape, ax, L.VDX_KIND_CONV, False, normalize, code, code, _signal(input_signal_range, shape[ax]),
+                      kop, code, broadcast)
+    es = vt.item_size
+    in_ptr, out_ptr, k_ptr = in_buf.ptr, out_buf.ptr, kbuf.ptr
+    in_end, out_end = in_ptr + total * es, out_ptr + ((kernel_num - 1) * ostride + total) * es
+    # the first kernel_num - 1 outputs must not overwrite the signal the later kernels read
+    overlap = in_ptr < out_end and out_ptr < in_end
+    stage = torch.empty(total, dtype=vt.torch_dtype, device=in_buf.tensor.device) if overlap else None
+
+    def launch(s):
+        src = in_ptr
+        if stage is not None:
+            L.convert(in_ptr, code, stage.data_ptr(), code, total, s)
+            src = stage.data_ptr()
+        for k in range(kernel_num):
+            plan.exec(src, out_ptr + k * ostride * es, k_ptr + k * kstride * es, s)
+
+    _record(graph, launch, (in_buf, out_buf, kbuf, stage))
 
 
 def convolve2D(buffer: Buffer, kernel: Buffer, kernel_map=None, buffer_shape=None, graph=None, print_shader=False,

@@ -14,6 +14,11 @@ libvdx implements; anything else raises NotImplementedError naming the map.
                read into a register k, register *= k         plain product
                register *= to_complex(scale[io_index])       real scale buffer
                (empty body)                                  no spectrum operation
+
+With kernel_num > 1 (vkdispatch/fft/shader_factories.py:166-193) a kernel
+map's read_from_buffer and an output map's write_to_buffer may index
+``io_index + mapped_kernel_index() * C``: kernel k then reads (or writes)
+C * k elements further along its buffer.
 """
 
 from __future__ import annotations
@@ -86,10 +91,42 @@ class _TraceOp:
 
     def read_from_buffer(self, buffer, register=None, io_index=None):
         name = register._name if isinstance(register, TraceRegister) else "reg"
-        self._events.append(("read", buffer.index, name, io_index is None))
+        stride = kernel_stride(io_index)
+        self._events.append(("read", buffer.index, name, stride is not None, stride or 0))
 
     def write_to_buffer(self, buffer, register=None, io_index=None):
-        self._events.append(("write", buffer.index, io_index is None))
+        stride = kernel_stride(io_index)
+        self._events.append(("write", buffer.index, stride is not None, stride or 0))
+
+
+def mapped_kernel_index():
+    """The kernel index of a multi-kernel convolution while its maps are
+    traced (a symbol to index buffers with), else None
+    (vkdispatch/fft/shader_factories.py:99-105)."""
+    return getattr(_tls, "kidx", None)
+
+
+def _is_io_index(e) -> bool:
+    return isinstance(e, vc.Sym) and e.op == "io_index"
+
+
+def kernel_stride(expr):
+    """Elements per kernel index of an io_index expression: 0 for None or
+    io_index itself, C for io_index + mapped_kernel_index() * C (either operand
+    order), None for any other expression."""
+    if expr is None or _is_io_index(expr):
+        return 0
+    if isinstance(expr, vc.Sym) and expr.op == "add" and len(expr.args) == 2:
+        a, b = expr.args
+        if _is_io_index(b):
+            a, b = b, a
+        if _is_io_index(a) and isinstance(b, vc.Sym) and b.op == "mul" and len(b.args) == 2:
+            x, y = b.args
+            if isinstance(y, vc.Sym) and y.op == "kidx":
+                x, y = y, x
+            if isinstance(x, vc.Sym) and x.op == "kidx" and isinstance(y, int) and y >= 0:
+                return y
+    return None
 
 
 def read_op():
@@ -120,6 +157,7 @@ def _trace(mf, role: str):
     types = mf.input_dtypes()
     bufs = [_TraceBuffer(i, t, events) for i, t in enumerate(types)]
     _tls.events, _tls.nreg = events, 0
+    _tls.kidx = vc.Sym("kidx")
     _tls.read = _TraceOp(events) if role in ("input", "kernel") else None
     _tls.write = _TraceOp(events) if role == "output" else None
     try:
@@ -129,7 +167,7 @@ def _trace(mf, role: str):
     except Exception as e:  # noqa: BLE001
         raise NotImplementedError(f"{role} map {mf.func.__name__} could not be traced: {e}") from e
     finally:
-        _tls.events = _tls.read = _tls.write = None
+        _tls.events = _tls.read = _tls.write = _tls.kidx = None
     return events, types
 
 
@@ -152,6 +190,7 @@ class IoMap:
     kind: str  # "complex" or "real"
     buffer: int  # index among the map's buffers
     var_type: object
+    stride: int = 0  # elements per kernel index (multi-kernel convolutions)
 
 
 @dataclass
@@ -159,12 +198,13 @@ class KernelMap:
     kind: str  # "conj_mul", "mul", "real_scale" or "identity"
     buffer: Optional[int]
     var_type: object
+    stride: int = 0  # elements per kernel index (multi-kernel convolutions)
 
 
 def classify_input(mf) -> IoMap:
     ev, types = _trace(mf, "input")
     name = mf.func.__name__
-    if len(ev) == 1 and ev[0][0] == "read" and ev[0][2] == "reg" and ev[0][3]:
+    if len(ev) == 1 and ev[0][0] == "read" and ev[0][2] == "reg" and ev[0][3] and ev[0][4] == 0:
         i = ev[0][1]
         if not types[i].is_complex:
             raise NotImplementedError(f"input map {name}: read_from_buffer needs a complex buffer")
@@ -184,7 +224,7 @@ def classify_output(mf) -> IoMap:
         i = ev[0][1]
         if not types[i].is_complex:
             raise NotImplementedError(f"output map {name}: write_to_buffer needs a complex buffer")
-        return IoMap("complex", i, types[i])
+        return IoMap("complex", i, types[i], ev[0][3])
     if len(ev) == 1 and ev[0][0] == "store" and _has(ev[0][2], "reg_real", "reg"):
         i = ev[0][1]
         if types[i] in (dt.float32, dt.float64):
@@ -197,16 +237,16 @@ def classify_kernel(mf) -> KernelMap:
     name = mf.func.__name__
     if not ev:
         return KernelMap("identity", None, None)
-    if len(ev) == 2 and ev[0][0] == "read" and ev[1][0] == "set" and ev[1][1] == "reg":
-        i, reg = ev[0][1], ev[0][2]
+    if len(ev) == 2 and ev[0][0] == "read" and ev[1][0] == "set" and ev[1][1] == "reg" and ev[0][3]:
+        i, reg, stride = ev[0][1], ev[0][2], ev[0][4]
         prod = ev[1][2]
         if isinstance(prod, vc.Sym) and prod.op == "cmul" and types[i].is_complex:
             a, b = prod.args
             if isinstance(a, TraceRegister) and a._name == "reg":
                 if isinstance(b, vc.Sym) and b.op == "conj" and b.args[0].args == (reg,):
-                    return KernelMap("conj_mul", i, types[i])
+                    return KernelMap("conj_mul", i, types[i], stride)
                 if isinstance(b, TraceRegister) and b._name == reg:
-                    return KernelMap("mul", i, types[i])
+                    return KernelMap("mul", i, types[i], stride)
     if len(ev) == 1 and ev[0][0] == "set" and ev[0][1] == "reg":
         prod = ev[0][2]
         if isinstance(prod, vc.Sym) and prod.op == "cmul" and _has(prod.args[1], "to_complex"):
