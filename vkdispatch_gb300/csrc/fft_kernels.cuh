@@ -335,6 +335,11 @@ struct FixPlan {
   }
 };
 
+template <class P>
+struct IsFixPlan : std::false_type {};
+template <int N_, int T_, class L, int MAXE_>
+struct IsFixPlan<FixPlan<N_, T_, L, MAXE_>> : std::true_type {};
+
 template <class Re>
 __device__ __forceinline__ Cx<Re>* smem_base() {
   extern __shared__ __align__(16) unsigned char vdx_smem_raw[];
@@ -510,6 +515,51 @@ __global__ void __launch_bounds__(1024) k_conv(FftArgs a) {
         }
       }
     }
+  });
+  P.template run<true, true>(v, pl, sm, tw);
+  store_output<Plan, true, S, Re>(P, pl, a, v);
+}
+
+// Strided fused convolution for CTAs of at most 256 threads: the kernel
+// spectrum is loaded into registers before the forward FFT, so its HBM
+// latency overlaps the forward passes instead of following them (the
+// registers it takes need the 256-thread launch bound).
+template <class Plan, class S, class Re, int KOP>
+__global__ void __launch_bounds__(256) k_conv_pf(FftArgs a) {
+  const Plan P(a.pp);
+  constexpr int MAXE = Plan::MAXE;
+  const Place<true> pl(a, P.T());
+  Cx<Re>* sm = smem_base<Re>();
+  const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
+  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0();
+  const S* ker = reinterpret_cast<const S*>(a.ker) + pl.ker0();
+  P.assume_t(pl.t);
+  const int n = P.n();
+  const bool kvalid = pl.tile_full || pl.valid;
+  Cx<Re> kr[MAXE];
+  P.template last<false>([&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    constexpr int B = MAXE / RR;
+    const int nb = n / RR;
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      const int j = pl.t + b * P.T();
+#pragma unroll
+      for (int r = 0; r < RR; ++r)
+        kr[b * RR + r] = (j < nb && kvalid) ? Conv<S, Re>::ld(ker + (j + r * nb) * pl.ps) : mk<Re>(Re(0), Re(0));
+    }
+  });
+  Cx<Re> v[MAXE];
+  gather_input<Plan, S, Re>(P, pl, a, v, in);
+  P.template run<false, false>(v, pl, sm, tw);
+  P.template last<false>([&](auto rc) {
+    constexpr int RR = decltype(rc)::value;
+    constexpr int B = MAXE / RR;
+#pragma unroll
+    for (int b = 0; b < B; ++b)
+#pragma unroll
+      for (int r = 0; r < RR; ++r)
+        v[b * RR + r] = KOP == 0 ? cmulc(v[b * RR + r], kr[b * RR + r]) : cmul(v[b * RR + r], kr[b * RR + r]);
   });
   P.template run<true, true>(v, pl, sm, tw);
   store_output<Plan, true, S, Re>(P, pl, a, v);

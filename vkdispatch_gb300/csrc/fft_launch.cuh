@@ -1,9 +1,22 @@
 // Template launcher shared by the per-storage-type translation units.
 #pragma once
 
+#include <cstdlib>
+
 #include "vdx_internal.h"
 
 namespace vdx {
+
+// Strided compile-time convolutions of <= 256-thread CTAs load the kernel
+// spectrum before the forward FFT (k_conv_pf) unless VDX_CONV_PREFETCH=0.
+inline bool conv_prefetch() {
+  static const bool on = [] {
+    const char* e = std::getenv("VDX_CONV_PREFETCH");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 
 // C2C with an optional fused element-wise operation (complex64 only):
 // variant 0 = none, 1 = input weight, 2 = weighted |out|^2 partials
@@ -31,6 +44,9 @@ cudaError_t launch_c2c(const FftArgs& a, const Launch& l, bool strided, int vari
 template <class Plan, int KOP, bool STRIDED, class S, class Re>
 cudaError_t launch_conv_layout(const FftArgs& a, const Launch& l, int variant) {
   constexpr bool C64 = std::is_same<S, Cx<float>>::value;
+  if constexpr (C64 && STRIDED && IsFixPlan<Plan>::value) {
+    if (variant == 0 && l.block.x <= 256 && conv_prefetch()) return enqueue(k_conv_pf<Plan, S, Re, KOP>, l, a);
+  }
   if constexpr (C64 && KOP == 0) {
     if (variant == 1) return enqueue(k_conv<Plan, STRIDED, S, S, Re, 0, 1>, l, a);
   }
