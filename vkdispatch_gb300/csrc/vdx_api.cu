@@ -332,13 +332,17 @@ int plan_fourstep(vdx_plan* p, long long inner, long long outer, int smem_optin)
     p->ws = nullptr;
     return fail(VDX_ERR_NOMEM, std::string("four-step workspace: ") + cudaGetErrorString(e));
   }
+  e = cudaMalloc(reinterpret_cast<void**>(&p->d_status), sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, sizeof(int));
+  if (e != cudaSuccess) {
+    p->d_status = nullptr;
+    return cuda_fail(e, "four-step status word");
+  }
   if (p->tensor_core) {
     // 128-point tiles of 16 (8-byte) or 32 (4-byte) columns, 128 threads
     if (N1 != 128 || N0 != 128 || ppA.M != ppB.M || (ppA.M != 16 && ppA.M != 32))
       return fail(VDX_ERR_UNSUPPORTED, "tensor-core stages need 128 x 128 tiles of 16 or 32 columns");
     e = tc_dft_operands(p->dev, p->op == OP_C2C_INV, &p->tc_bmat);
-    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->d_status), sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, sizeof(int));
     if (e != cudaSuccess) return cuda_fail(e, "tensor-core plan set-up");
     p->blockA = p->blockB = dim3(128);
     p->smemA = p->smemB = tc_pass_smem(ppA.M);
@@ -402,6 +406,16 @@ int plan_conv2d_real(const vdx_fft_desc& d, vdx_plan** plan) {
   return VDX_OK;
 }
 
+// Four-step passes of strided axes stage their input tiles with TMA tensor
+// copies where fourstep_tma_ok allows it, unless VDX_FOURSTEP_TMA=0.
+bool fourstep_tma() {
+  static const bool on = [] {
+    const char* e = std::getenv("VDX_FOURSTEP_TMA");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 cudaError_t exec_fourstep(const vdx_plan* p, const void* in, void* out, cudaStream_t s) {
   const long long N = p->N, N0 = p->N0, N1 = p->N1, inner = p->inner, outer = p->outer;
   const size_t sb = store_bytes(p->store);
@@ -431,9 +445,11 @@ cudaError_t exec_fourstep(const vdx_plan* p, const void* in, void* out, cudaStre
         A.ncols = (int)Cc;
         A.col_tiles = (int)((Cc + MA - 1) / MA);
         A.tw_from_batch = 1;
+        A.nbatch = Oc * N0;
+        A.status = p->d_status;
         la.grid = dim3((unsigned)(Oc * N0 * A.col_tiles));
         e = p->tensor_core ? launch_fourstep_pass_tc(A, la, p->store, inv, 1, p->tc_bmat, p->d_status)
-                           : launch_fourstep_pass(A, la, p->store, inv, 1);
+                           : launch_fourstep_pass(A, la, p->store, inv, 1, fourstep_tma());
         if (e != cudaSuccess) return e;
         FsArgs B = p->fsB;
         B.in = p->ws;
@@ -448,9 +464,11 @@ cudaError_t exec_fourstep(const vdx_plan* p, const void* in, void* out, cudaStre
         B.out_cs = 1;
         B.ncols = (int)Cc;
         B.col_tiles = (int)((Cc + MB - 1) / MB);
+        B.nbatch = Oc * N1;
+        B.status = p->d_status;
         lb.grid = dim3((unsigned)(Oc * N1 * B.col_tiles));
         e = p->tensor_core ? launch_fourstep_pass_tc(B, lb, p->store, inv, 0, p->tc_bmat, p->d_status)
-                           : launch_fourstep_pass(B, lb, p->store, inv, 0);
+                           : launch_fourstep_pass(B, lb, p->store, inv, 0, fourstep_tma());
         if (e != cudaSuccess) return e;
       }
     }
@@ -473,9 +491,11 @@ cudaError_t exec_fourstep(const vdx_plan* p, const void* in, void* out, cudaStre
     A.ncols = (int)N0;
     A.col_tiles = (int)((N0 + MA - 1) / MA);
     A.tw_from_batch = 0;
+    A.nbatch = Rr;
+    A.status = p->d_status;
     la.grid = dim3((unsigned)(Rr * A.col_tiles));
     e = p->tensor_core ? launch_fourstep_pass_tc(A, la, p->store, inv, 2, p->tc_bmat, p->d_status)
-                       : launch_fourstep_pass(A, la, p->store, inv, 2);
+                       : launch_fourstep_pass(A, la, p->store, inv, 2, false);
     if (e != cudaSuccess) return e;
     FsArgs B = p->fsB;
     B.in = p->ws;
@@ -490,9 +510,11 @@ cudaError_t exec_fourstep(const vdx_plan* p, const void* in, void* out, cudaStre
     B.out_cs = 1;
     B.ncols = (int)N1;
     B.col_tiles = (int)((N1 + MB - 1) / MB);
+    B.nbatch = Rr;
+    B.status = p->d_status;
     lb.grid = dim3((unsigned)(Rr * B.col_tiles));
     e = p->tensor_core ? launch_fourstep_pass_tc(B, lb, p->store, inv, 0, p->tc_bmat, p->d_status)
-                       : launch_fourstep_pass(B, lb, p->store, inv, 0);
+                       : launch_fourstep_pass(B, lb, p->store, inv, 0, false);
     if (e != cudaSuccess) return e;
   }
   return e;

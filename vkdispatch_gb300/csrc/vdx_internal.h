@@ -65,9 +65,16 @@ struct FsArgs {
   int ncols, col_tiles;
   int tw_from_batch;  // pass A: b0 is b % split (strided axes) or the column (contiguous axes)
   float scale;
+  int* status;        // TMA-staged passes: set to 1 if a tile load's completion wait gives up
+  long long nbatch;   // batches of this launch (grid = nbatch * col_tiles)
 };
-// mode 0: plain store; 1: twiddle, unit-stride columns; 2: twiddle, transposed store (out_ps == 1)
-cudaError_t launch_fourstep_pass(const FsArgs& a, const Launch& l, int store, bool inv, int mode);
+// mode 0: plain store; 1: twiddle, unit-stride columns; 2: twiddle, transposed store (out_ps == 1).
+// With tma = true the input tiles arrive by one TMA bulk-tensor copy each
+// when the geometry allows it (see fourstep_tma_ok); otherwise by loads.
+cudaError_t launch_fourstep_pass(const FsArgs& a, const Launch& l, int store, bool inv, int mode, bool tma = false);
+// Whether a pass's input tiles can be TMA copies: short length <= 256 (one
+// box), 16-byte row and batch strides, 16-byte aligned base and columns.
+bool fourstep_tma_ok(const FsArgs& a, int store);
 // The same pass with the 128-point short transforms on the tensor cores
 // (fft_tc.cu); a.pp.n must be 128 and a.pp.M 16 or 32.  bmat = the DFT
 // operand image from tc_dft_operands; *status is set to 1 if an MMA
