@@ -153,3 +153,24 @@ def test_fused_ops_rejected_on_fourstep_plans():
     ops.in_weight_scale = 1.0
     with pytest.raises(ValueError):
         p.exec_ops(t.data_ptr(), t.data_ptr(), None, ops, torch.cuda.current_stream().cuda_stream)
+
+
+@pytest.mark.parametrize("vt", [vd.complexbf16, vd.complex32])
+@pytest.mark.parametrize("shape,axis,ws_mb", [((16384, 40), 0, None), ((3, 16384, 36), 1, None),
+                                              ((16384, 100), 0, 1)])
+def test_half_storage_strided_tiles(vt, shape, axis, ws_mb):
+    """Strided axes with 4-byte storage stage their tiles with TMA copies:
+    partial last tiles (zero-filled columns), outer batches (rank-4 maps) and
+    chunked workspaces (moved base pointers)."""
+    rng = np.random.default_rng(sum(shape) + axis)
+    x = crandn(rng, shape) * 0.25
+    buf = vd.Buffer(shape, vt)
+    buf.write(x)
+    q = buf.read(0).astype(np.complex128)
+    with _env(VDX_FOURSTEP_WS_MB=ws_mb):
+        P.cache_clear()
+        vd.fft.fft(buf, axis=axis)
+    got = buf.read(0)
+    tol = 5e-3 if vt == vd.complexbf16 else 1.2e-3
+    assert rel_l2(got, np.fft.fft(q, axis=axis)) < tol
+    P.cache_clear()
