@@ -107,6 +107,18 @@ typedef struct vdx_fft_desc {
  * rule (vkdispatch/fft/config.py:102-190).
  */
 #define VDX_FFT_FLAG_AUTOTUNE 2
+/*
+ * VDX_FFT_FLAG_BLUESTEIN: C2C axes whose length has a prime factor above 13
+ * (which the reference rejects, vkdispatch/fft/prime_utils.py:6-10) are
+ * planned as Bluestein chirp-z transforms instead of failing: a chirp
+ * multiply into a zero-padded workspace of length M (the power of two >=
+ * 2N - 1), one fused length-M convolution against the precomputed
+ * conj(FFT_M(chirp)), and a chirp multiply out.  The chirps are built in FP64
+ * from the exact integer n^2 mod 2N.  Limits: M <= 16384 (fp32 compute) or
+ * 8192 (fp64).  Without the flag such lengths fail with VDX_ERR_UNSUPPORTED,
+ * as in the reference.
+ */
+#define VDX_FFT_FLAG_BLUESTEIN 4
 
 typedef struct vdx_plan vdx_plan;
 

@@ -30,6 +30,7 @@ VDX_KIND_C2C, VDX_KIND_R2C, VDX_KIND_C2R, VDX_KIND_CONV, VDX_KIND_CONV2D_REAL = 
 VDX_KOP_MUL_CONJ, VDX_KOP_MUL = range(2)
 VDX_FFT_FLAG_TENSOR_CORE = 1
 VDX_FFT_FLAG_AUTOTUNE = 2
+VDX_FFT_FLAG_BLUESTEIN = 4
 
 # reductions and maps
 VDX_RED_ADD, VDX_RED_MUL, VDX_RED_MIN, VDX_RED_MAX, VDX_RED_AND, VDX_RED_OR, VDX_RED_XOR = range(7)

@@ -217,6 +217,13 @@ struct vdx_plan {
   Tune tune;
   float tuned_ms = 0.f;
   int tuned_candidates = 0;
+  // Bluestein (bluestein.cu): chirp w, kernel slab conj(FFT_M(b)), workspace, conv plan
+  bool bluestein = false;
+  int bs_M = 0;
+  void* bs_w = nullptr;
+  void* bs_K = nullptr;
+  void* bs_ws = nullptr;
+  vdx_plan* bs_conv = nullptr;
   // one-launch convolve2DR (fft_conv2d.cu)
   int c2_H = 0, c2_W = 0;
   long long c2_images = 0;
@@ -224,6 +231,10 @@ struct vdx_plan {
   ~vdx_plan() {
     if (ws) cudaFree(ws);
     if (d_status) cudaFree(d_status);
+    if (bs_w) cudaFree(bs_w);
+    if (bs_K) cudaFree(bs_K);
+    if (bs_ws) cudaFree(bs_ws);
+    delete bs_conv;
   }
 };
 
@@ -524,6 +535,91 @@ cudaError_t exec_fourstep(const vdx_plan* p, const void* in, void* out, cudaStre
 
 namespace {
 
+int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan);
+
+// Bluestein plan (bluestein.cu): three launches per execution.
+int plan_bluestein(const vdx_fft_desc& d, long long inner, long long outer, int N, int st, bool f64,
+                   vdx_plan** plan) {
+  int M = 1;
+  while (M < 2 * N - 1) M <<= 1;
+  const int mmax = f64 ? 8192 : 16384;
+  if (M > mmax)
+    return fail(VDX_ERR_UNSUPPORTED, "Bluestein length " + std::to_string(N) + " needs a " + std::to_string(M) +
+                                         "-point convolution (limit " + std::to_string(mmax) + ")");
+  auto* p = new vdx_plan();
+  p->d = d;
+  p->op = d.inverse ? OP_C2C_INV : OP_C2C_FWD;
+  p->store = st;
+  p->f64 = f64;
+  p->N = N;
+  p->bluestein = true;
+  p->bs_M = M;
+  p->inner = inner;
+  p->outer = outer;
+  cudaError_t e = cudaGetDevice(&p->dev);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(e, "cudaGetDevice");
+  }
+  const int cx = f64 ? VDX_C128 : VDX_C64;
+  vdx_fft_desc dc;
+  std::memset(&dc, 0, sizeof(dc));
+  dc.ndim = 3;
+  dc.shape[0] = outer;
+  dc.shape[1] = M;
+  dc.shape[2] = inner;
+  dc.axis = 1;
+  dc.kind = VDX_KIND_CONV;
+  dc.normalize = 1;
+  dc.io_type = dc.compute_type = dc.kernel_type = cx;
+  dc.signal_lo = dc.signal_hi = -1;
+  dc.kernel_op = VDX_KOP_MUL_CONJ;
+  dc.kernel_broadcast = 1;
+  int rc = create_plan(&dc, Tune{}, &p->bs_conv);
+  if (rc != VDX_OK) {
+    delete p;
+    return rc;
+  }
+  const size_t es = f64 ? 16 : 8;
+  void* b = nullptr;
+  vdx_plan* tmp = nullptr;
+  cudaStream_t s = nullptr;
+  e = cudaMalloc(&p->bs_w, size_t(N) * es);
+  if (e == cudaSuccess) e = cudaMalloc(&b, size_t(M) * es);
+  if (e == cudaSuccess) e = cudaMalloc(&p->bs_K, size_t(M) * size_t(inner) * es);
+  if (e == cudaSuccess) e = cudaMalloc(&p->bs_ws, size_t(outer) * size_t(M) * size_t(inner) * es);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = launch_chirp_tables(p->bs_w, b, N, M, d.inverse ? 1 : -1, f64, s);
+  if (e == cudaSuccess) {
+    vdx_fft_desc df;
+    std::memset(&df, 0, sizeof(df));
+    df.ndim = 2;
+    df.shape[0] = 1;
+    df.shape[1] = M;
+    df.axis = 1;
+    df.kind = VDX_KIND_C2C;
+    df.io_type = df.compute_type = cx;
+    df.signal_lo = df.signal_hi = -1;
+    rc = create_plan(&df, Tune{}, &tmp);
+    if (rc == VDX_OK) rc = vdx_fft_exec(tmp, b, b, nullptr, s);  // B = FFT_M(b)
+    if (rc == VDX_OK) e = launch_conj_slab(p->bs_K, b, M, inner, f64, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  delete tmp;
+  if (s) cudaStreamDestroy(s);
+  if (b) cudaFree(b);
+  if (rc != VDX_OK) {
+    delete p;
+    return rc;
+  }
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(e, "Bluestein plan set-up");
+  }
+  *plan = p;
+  return VDX_OK;
+}
+
 int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
   if (!desc || !plan) return fail(VDX_ERR_INVALID, "desc and plan must be non-NULL");
   *plan = nullptr;
@@ -555,7 +651,7 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
       return fail(VDX_ERR_UNSUPPORTED, "VDX_KOP_MUL convolutions need complex64 storage");
   }
   if (real && (st == ST_BF16)) return fail(VDX_ERR_UNSUPPORTED, "real transforms support complex64/complex32/complex128");
-  if (d.flags & ~(VDX_FFT_FLAG_TENSOR_CORE | VDX_FFT_FLAG_AUTOTUNE))
+  if (d.flags & ~(VDX_FFT_FLAG_TENSOR_CORE | VDX_FFT_FLAG_AUTOTUNE | VDX_FFT_FLAG_BLUESTEIN))
     return fail(VDX_ERR_INVALID, "unknown bits in desc.flags");
   if (d.normalize < 0 || d.normalize > 2) return fail(VDX_ERR_INVALID, "normalize must be 0, 1 or 2");
 
@@ -592,7 +688,9 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
   std::string why;
   if (!factor_radices(n, maxe, p->radices, why)) {
     delete p;
-    return fail(VDX_ERR_UNSUPPORTED, why);
+    if ((d.flags & VDX_FFT_FLAG_BLUESTEIN) && d.kind == VDX_KIND_C2C && lo == 0 && hi == N)
+      return plan_bluestein(d, inner, outer, N, st, f64, plan);
+    return fail(VDX_ERR_UNSUPPORTED, why + " (VDX_FFT_FLAG_BLUESTEIN plans such lengths)");
   }
   if (tune.order == 1) std::reverse(p->radices.begin(), p->radices.end());
 
@@ -1035,6 +1133,12 @@ int vdx_fft_plan_describe(const vdx_plan* p, char* buf, size_t n) {
   if (!p || !buf || n == 0) return fail(VDX_ERR_INVALID, "plan and buf must be non-NULL");
   std::string r;
   for (size_t i = 0; i < p->radices.size(); ++i) r += (i ? "x" : "") + std::to_string(p->radices[i]);
+  if (p->bluestein) {
+    std::snprintf(buf, n,
+                  "{\"op\": \"%s\", \"N\": %d, \"bluestein\": %d, \"strided\": %s, \"autotuned\": false}",
+                  p->op == OP_C2C_INV ? "c2c_inv" : "c2c_fwd", p->N, p->bs_M, p->inner > 1 ? "true" : "false");
+    return VDX_OK;
+  }
   if (p->fourstep) {
     std::snprintf(buf, n,
                   "{\"op\": \"%s\", \"N\": %d, \"fourstep\": [%d, %d], \"strided\": %s, "
@@ -1093,6 +1197,19 @@ int exec_plan(const vdx_plan* p, const void* in, void* out, const void* kernel, 
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   if (dev != p->dev) return fail(VDX_ERR_INVALID, "plan was created on another device");
+  if (p->bluestein) {
+    if (ops && (ops->in_weight || ops->spec_out || ops->loss_weight))
+      return fail(VDX_ERR_UNSUPPORTED, "fused operations are not available on Bluestein plans");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    e = launch_bluestein_io(true, p->store, in, p->bs_ws, p->bs_w, p->outer, p->N, p->bs_M, p->inner, 1.0, s);
+    if (e != cudaSuccess) return cuda_fail(e, "Bluestein chirp-in launch");
+    const int rc = exec_plan(p->bs_conv, p->bs_ws, p->bs_ws, p->bs_K, nullptr, stream);
+    if (rc != VDX_OK) return rc;
+    e = launch_bluestein_io(false, p->store, out, p->bs_ws, p->bs_w, p->outer, p->N, p->bs_M, p->inner,
+                            norm_scale(p->d.normalize, p->N), s);
+    if (e != cudaSuccess) return cuda_fail(e, "Bluestein chirp-out launch");
+    return VDX_OK;
+  }
   if (p->fourstep) {
     if (ops && (ops->in_weight || ops->spec_out || ops->loss_weight))
       return fail(VDX_ERR_UNSUPPORTED, "fused operations are not available on four-step (long-axis) plans");

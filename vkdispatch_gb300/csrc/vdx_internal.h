@@ -95,6 +95,15 @@ struct Conv2dArgs {
   const Cx<float>* tw_col;  // W_H^k, k < H
   float col_scale, row_scale;
 };
+// Bluestein transforms (bluestein.cu): chirp tables w (N) and b (M), the
+// conj(FFT(b)) kernel slab replicated over `inner` columns, and the
+// chirp-in (zero-padded, to the (outer, M, inner) workspace) / chirp-out
+// (cropped, scaled) element-wise launches.
+cudaError_t launch_chirp_tables(void* w, void* b, int N, int M, int sign, bool f64, cudaStream_t s);
+cudaError_t launch_conj_slab(void* K, const void* B, int M, long long inner, bool f64, cudaStream_t s);
+cudaError_t launch_bluestein_io(bool in_phase, int store, const void* x, void* ws, const void* w, long long outer,
+                                int N, int M, long long inner, double scale, cudaStream_t s);
+
 bool conv2d_real_supported(int H, int W);
 cudaError_t conv2d_real_max_clusters(int H, int W, int* count);
 cudaError_t launch_conv2d_real(const Conv2dArgs& a, int H, int W, long long images, int kop, cudaStream_t s);

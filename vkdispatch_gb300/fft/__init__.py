@@ -22,4 +22,12 @@ from .functions import (  # noqa: F401
     transpose,
 )
 from .maps import mapped_kernel_index, read_op, write_op  # noqa: F401
-from .plan import autotune, autotune_load, autotune_save, autotune_stats, get_plan, tensor_core_stages  # noqa: F401
+from .plan import (  # noqa: F401
+    autotune,
+    autotune_load,
+    autotune_save,
+    autotune_stats,
+    bluestein,
+    get_plan,
+    tensor_core_stages,
+)

@@ -37,6 +37,19 @@ def autotune(enabled: bool = True):
         _tls.tune = old
 
 
+@contextlib.contextmanager
+def bluestein(enabled: bool = True):
+    """Within the block, C2C axes whose length has a prime factor above 13
+    (which the reference rejects) are planned as Bluestein chirp-z
+    transforms instead of raising.  Per thread."""
+    old = getattr(_tls, "bluestein", False)
+    _tls.bluestein = bool(enabled)
+    try:
+        yield
+    finally:
+        _tls.bluestein = old
+
+
 def autotune_stats() -> Tuple[int, int]:
     """(cached choices, candidate searches run) of this process."""
     a, b = ctypes.c_int64(), ctypes.c_int64()
@@ -126,6 +139,8 @@ def get_plan(
             flags = L.VDX_FFT_FLAG_TENSOR_CORE
         if getattr(_tls, "tune", False):
             flags |= L.VDX_FFT_FLAG_AUTOTUNE
+        if getattr(_tls, "bluestein", False) and kind == L.VDX_KIND_C2C:
+            flags |= L.VDX_FFT_FLAG_BLUESTEIN
     key = (dev, tuple(shape), axis, kind, bool(inverse), int(normalize), io_type, compute_type, signal_range,
            kernel_op, kernel_type, bool(kernel_broadcast), int(flags))
     p = _cache.get(key)
