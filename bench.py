@@ -145,6 +145,28 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(ms, dist=None, device="cuda"):
+    """The slowest replica's time: the job's step ends when every rank's does."""
+    if dist is None:
+        return ms
+    import torch
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gbps(world, step_bytes, ms):
+    """Whole-job throughput of `world` replicas that each move step_bytes per step."""
+    return world * step_bytes / (ms * 1e-3) / 1e9
+
+
+def reference_arm_runs_here(rank):
+    """Under torchrun the CPU reference arm runs on rank 0 only; the other
+    ranks exit without work."""
+    return rank == 0
+
+
 def run_ours(args):
     """Every plan of this arm is autotuned when it is created (vd.fft.autotune:
     the fastest of the candidate CTA sizes / tile widths / radix orders, timed
@@ -233,12 +255,8 @@ def _run_ours(args):
         per["conv"].append(e[1].elapsed_time(e[2]))
         per["c2r"].append(e[2].elapsed_time(e[3]))
         steps_ms.append(e[0].elapsed_time(e[3]))
-    ms = statistics.mean(steps_ms)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * STEP_BYTES / (ms * 1e-3) / 1e9
+    ms = max_over_ranks(statistics.mean(steps_ms), dist)
+    value = whole_job_gbps(world, STEP_BYTES, ms)
 
     # dominant kernel roofline
     mean_k = {k: statistics.mean(v) for k, v in per.items()}
@@ -289,7 +307,7 @@ def _run_ours(args):
     s_out.wait_stream(s_c)
     e_s[1].record(s_out)
     torch.cuda.synchronize()
-    e2e_ms = e_s[0].elapsed_time(e_s[1]) / KE
+    e2e_ms = max_over_ranks(e_s[0].elapsed_time(e_s[1]) / KE, dist)
     last = h_out[(KE - 1) % 2][..., :W].numpy()
     e2e_err = float(np.linalg.norm((last - ref).ravel()) / np.linalg.norm(ref.ravel()))
     e2e_bytes = h_in.numel() * 4
@@ -338,7 +356,7 @@ def _run_ours(args):
             },
             "cpu_baseline": cpu,
             "e2e": {
-                "value": round(world * STEP_BYTES / (e2e_ms * 1e-3) / 1e9, 2),
+                "value": round(whole_job_gbps(world, STEP_BYTES, e2e_ms), 2),
                 "unit": "GB/s",
                 "ms_per_step": round(e2e_ms, 4),
                 "h2d_bytes_per_step": e2e_bytes,
@@ -796,7 +814,7 @@ def cpu_baseline(images, kernel, budget_s=8.0):
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    if not reference_arm_runs_here(rank):
         return
     from oracle import ref
 
