@@ -125,7 +125,8 @@ __device__ __forceinline__ void run_unit(const BatchArgs& a, const WorkUnit* __r
       return src[pos * src_pt];
     });
   });
-  run_passes<MAXE, INV>(v, pp, false, pl, sm, tw);
+  // row units keep each transform inside one warp when T divides 32
+  run_passes<MAXE, INV>(v, pp, false, pl, sm, tw, !cols && warp_sized(T));
   Cx<float>* dst = (kind == UK_COLS ? a.ws : a.data) + wu.dst + pl.m * wu.dst_slot;
   const long long dst_pt = wu.dst_pt;
   const bool twiddle = cols;

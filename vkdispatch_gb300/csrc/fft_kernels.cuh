@@ -114,6 +114,28 @@ struct Place {
   }
 };
 
+// A placement whose transforms each occupy consecutive threads (t fastest)
+// keeps every transform of T | 32 threads inside one warp, with shared-memory
+// slots of its own: its exchanges between passes need only warp
+// synchronisation.  Strided column tiles spread a transform over warps.
+template <class PL>
+struct WarpLocal : std::false_type {};
+template <>
+struct WarpLocal<Place<false>> : std::true_type {};
+
+__host__ __device__ constexpr bool warp_sized(int T) { return T >= 1 && T <= 32 && 32 % T == 0; }
+
+template <bool WARP>
+__device__ __forceinline__ void xsync() {
+  if constexpr (WARP) __syncwarp();
+  else __syncthreads();
+}
+// runtime scope; `warp` must be the same for the whole CTA
+__device__ __forceinline__ void xsync(bool warp) {
+  if (warp) __syncwarp();
+  else __syncthreads();
+}
+
 template <int V>
 using IC = std::integral_constant<int, V>;
 
@@ -205,7 +227,7 @@ __device__ __forceinline__ void scatter(const Cx<Re>* v, int nb, int T, int t, i
 // holding natural-order outputs laid out for the last executed radix.
 template <int MAXE, bool INV, class PL, class Re>
 __device__ __forceinline__ void run_passes(Cx<Re>* v, const PassPlan& pp, bool reversed, const PL& pl,
-                                           Cx<Re>* sm, const Cx<Re>* tw) {
+                                           Cx<Re>* sm, const Cx<Re>* tw, bool warp = false) {
   const int n = pp.n, P = pp.npass, T = pp.T, t = pl.t;
   int ns = 1;
   for (int q = 0; q < P; ++q) {
@@ -217,12 +239,12 @@ __device__ __forceinline__ void run_passes(Cx<Re>* v, const PassPlan& pp, bool r
       constexpr int RR = decltype(rc)::value;
       butterflies<RR, MAXE, INV, Re>(v, n / RR, T, t, ns, n, tw);
       if (more) {
-        __syncthreads();
+        xsync(warp);
         scatter<RR, MAXE, Re>(v, n / RR, T, t, ns, [&](int pos, Cx<Re> val) { sm[pl.sidx(pp, pos)] = val; });
       }
     });
     if (more) {
-      __syncthreads();
+      xsync(warp);
       const int R2 = pp.radix[reversed ? P - 2 - q : q + 1];
       radix_dispatch(R2, [&](auto rc) {
         constexpr int RR = decltype(rc)::value;
@@ -286,17 +308,18 @@ struct DynPlan {
   }
   template <bool INV, bool REV, class PL, class Re>
   __device__ __forceinline__ void run(Cx<Re>* v, const PL& pl, Cx<Re>* sm, const Cx<Re>* tw) const {
-    run_passes<MAXE, INV>(v, pp, REV, pl, sm, tw);
+    run_passes<MAXE, INV>(v, pp, REV, pl, sm, tw, WarpLocal<PL>::value && warp_sized(pp.T));
   }
 };
 
 template <int N, int T, int MAXE, bool INV, class Re, class PL, int NS, int R, int... Rest>
 __device__ __forceinline__ void chain(Cx<Re>* v, const PassPlan& pp, const PL& pl, Cx<Re>* sm, const Cx<Re>* tw) {
+  constexpr bool W = WarpLocal<PL>::value && warp_sized(T);
   butterflies<R, MAXE, INV, Re>(v, N / R, T, pl.t, NS, N, tw);
   if constexpr (sizeof...(Rest) > 0) {
-    __syncthreads();
+    xsync<W>();
     scatter<R, MAXE, Re>(v, N / R, T, pl.t, NS, [&](int pos, Cx<Re> val) { sm[pl.sidx(pp, pos)] = val; });
-    __syncthreads();
+    xsync<W>();
     constexpr int R2 = RFirst<RList<Rest...>>::value;
     gather<R2, MAXE, Re>(v, N / R2, T, pl.t, [&](int pos) { return sm[pl.sidx(pp, pos)]; });
     chain<N, T, MAXE, INV, Re, PL, NS * R, Rest...>(v, pp, pl, sm, tw);
@@ -604,13 +627,14 @@ __global__ void __launch_bounds__(1024) k_r2c_even(FftArgs a) {
     });
   });
   P.template run<false, false>(v, pl, sm, tw);
-  __syncthreads();
+  const bool wsync = warp_sized(P.T());  // rows: the exchange below stays inside the row's warp
+  xsync(wsync);
   P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
     each_natural<RR, MAXE, Re>(v, n / RR, P.T(), pl.t,
                                [&](int pos, Cx<Re> val) { sm[pl.sidx_plain(pp, pos)] = val; });
   });
-  __syncthreads();
+  xsync(wsync);
   const Re half = Re(0.5);
   const bool wr = pl.tile_full || pl.valid;
   P.template last<false>([&](auto rc) {
@@ -672,7 +696,7 @@ __global__ void __launch_bounds__(1024) k_c2r_even(FftArgs a) {
     x.y = Re(0);
     sm[pl.sidx_plain(pp, n)] = x;
   }
-  __syncthreads();
+  xsync(warp_sized(P.T()));  // rows: the exchange stays inside the row's warp
   P.template first<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
     gather<RR, MAXE, Re>(v, n / RR, P.T(), pl.t, [&](int k) {
