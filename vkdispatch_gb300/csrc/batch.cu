@@ -306,7 +306,7 @@ int vdx_batch_plan_create(const vdx_batch_item* items, int nitems, int inverse, 
     const int T = threads_for(radices, n);
     if (T > cta) return -2;
     int M = std::max(1, cta / T);
-    if (cols) M = std::min(M, 16);
+    if (cols) M = std::min(M, 64);  // column tiles: up to 64 columns (256-byte row segments per warp)
     M = std::min(M, std::max(1, slots_max));
     const int npad = npad_of(n);
     // leave room for the kernel's static shared variables
