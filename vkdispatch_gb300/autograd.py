@@ -27,13 +27,14 @@ from typing import Optional, Sequence
 import torch
 
 from . import _lib as L
+from . import graph as G
 from .fft import plan as P
 
 _IO = {torch.complex64: (L.VDX_C64, L.VDX_C64), torch.complex128: (L.VDX_C128, L.VDX_C128)}
 
 
 def _stream() -> int:
-    return int(torch.cuda.current_stream().cuda_stream)
+    return G.current_stream_handle()
 
 
 def _check_tensor(t: torch.Tensor, name: str) -> None:

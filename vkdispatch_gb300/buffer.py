@@ -9,6 +9,7 @@ reference's checks: C-contiguous, dtype match, read-only flag.
 
 from __future__ import annotations
 
+import math
 import typing
 from typing import Optional, Tuple
 
@@ -20,9 +21,15 @@ from . import dtypes as dt
 MAX_ELEMENTS = 2**30  # the reference caps buffers at 2^30 elements (buffer.py:86-87)
 
 
+_cuda_checked = False
+
+
 def _device() -> torch.device:
-    if not torch.cuda.is_available():
-        raise RuntimeError("vkdispatch_gb300 needs a CUDA device (no CPU fallback)")
+    global _cuda_checked
+    if not _cuda_checked:
+        if not torch.cuda.is_available():
+            raise RuntimeError("vkdispatch_gb300 needs a CUDA device (no CPU fallback)")
+        _cuda_checked = True
     return torch.device("cuda", torch.cuda.current_device())
 
 
@@ -35,7 +42,7 @@ class Buffer:
             raise ValueError("Buffer shape must have 1 to 4 dimensions")
         if any(s < 1 for s in shape):
             raise ValueError("Buffer dimensions must be positive")
-        size = int(np.prod(shape))
+        size = math.prod(shape)
         if size > MAX_ELEMENTS:
             raise ValueError(f"Buffer of {size} elements exceeds the 2^30 element limit")
         self.shape = shape

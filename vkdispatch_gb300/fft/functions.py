@@ -9,6 +9,7 @@ cached plan and records one launch into the graph (immediate by default).
 
 from __future__ import annotations
 
+import math
 import os
 from typing import Optional, Tuple, Union
 
@@ -135,7 +136,7 @@ def _staged(plan_fn, out_buf, out_kind, in_buf, in_kind, shape, compute, graph, 
 
     ct = _compute_torch(compute)
     code = L.VDX_C128 if ct == torch.complex128 else L.VDX_C64
-    count = int(np.prod(shape))
+    count = math.prod(shape)
     in_direct = in_kind == "complex" and in_buf.var_type.vdx_code == code
     out_direct = out_kind == "complex" and out_buf.var_type.vdx_code == code
     stage_in = None if in_direct else torch.empty(count, dtype=ct, device=in_buf.tensor.device)
@@ -250,7 +251,7 @@ def fft(
             raise ValueError(f"R2C buffer of shape {buf.shape} does not match real shape {buffer_shape}")
         kind = L.VDX_KIND_C2R if inverse else L.VDX_KIND_R2C
     else:
-        if int(np.prod(buffer_shape)) > buf.size:
+        if math.prod(buffer_shape) > buf.size:
             raise ValueError(f"buffer_shape {buffer_shape} exceeds the buffer size {buf.size}")
         kind = L.VDX_KIND_C2C
     plan = P.get_plan(
@@ -417,8 +418,8 @@ def convolve(
         raise ValueError("kernel_type/output_type must match the buffers' types")
     compute = resolve_compute_precision([out_t, in_t, k_t], compute_type)
     ax = _norm_axis(axis, len(buffer_shape))
-    total = int(np.prod(buffer_shape))
-    slab = int(np.prod(buffer_shape[ax:]))
+    total = math.prod(buffer_shape)
+    slab = math.prod(buffer_shape[ax:])
     broadcast = bool(kernel_inner_only)
     if not broadcast and ker.size < total:
         if ker.size >= slab:
@@ -464,7 +465,7 @@ def _convolve_mapped(buffers, kernel_map, buffer_shape, graph, axis, normalize, 
     shape = tuple(int(x) for x in (buffer_shape if buffer_shape is not None else buffers[0].shape))
     ax = _norm_axis(axis, len(shape))
     sr = _signal(input_signal_range, shape[ax])
-    total, slab = int(np.prod(shape)), int(np.prod(shape[ax:]))
+    total, slab = math.prod(shape), math.prod(shape[ax:])
     if km.kind == "identity":
         # no spectrum operation: the forward and inverse transforms cancel up to 1/N
         def plan_fn(code):
@@ -553,7 +554,7 @@ def _convolve_multi(buffers, kernel_map, kernel_num, buffer_shape, graph, axis, 
         raise NotImplementedError("multi-kernel convolutions compute in their storage precision")
     shape = tuple(int(x) for x in (buffer_shape if buffer_shape is not None else in_buf.shape))
     ax = _norm_axis(axis, len(shape))
-    total, slab = int(np.prod(shape)), int(np.prod(shape[ax:]))
+    total, slab = math.prod(shape), math.prod(shape[ax:])
     broadcast = bool(kernel_inner_only) or (kbuf.size - (kernel_num - 1) * kstride < total)
     need_k = (kernel_num - 1) * kstride + (slab if broadcast else total)
     if kbuf.size < need_k:
@@ -612,8 +613,8 @@ def _conv2d_fused(buffer, kernel, kernel_inner_only, normalize, graph, print_sha
     if os.environ.get("VDX_FUSED_CONV2D", "0") != "1":
         return False
     real_shape = tuple(int(x) for x in buffer.real_shape)
-    total = int(np.prod(buffer.shape))
-    slab = int(np.prod(buffer.shape[-2:]))
+    total = math.prod(buffer.shape)
+    slab = math.prod(buffer.shape[-2:])
     broadcast = bool(kernel_inner_only)
     if not broadcast and kernel.size < total:
         if kernel.size < slab:
@@ -662,7 +663,7 @@ def get_transposed_size(buffer_shape: Tuple, axis: int = None, compute_type=dt.c
     """Elements of the kernel layout that ``transpose`` produces.  This build
     reads kernel spectra in natural order, so the layout is the spectrum
     itself."""
-    return int(np.prod(buffer_shape))
+    return math.prod(buffer_shape)
 
 
 def transpose(in_buffer: Buffer, conv_shape: Tuple = None, axis: int = None, out_buffer: Buffer = None,

@@ -21,11 +21,19 @@ import torch
 _tls = threading.local()
 
 
+_raw_stream = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+_get_device = getattr(torch._C, "_cuda_getDevice", None)
+
+
 def current_stream_handle() -> int:
-    """The cudaStream_t (as int) launches go to."""
+    """The cudaStream_t (as int) launches go to: the capture override, else
+    the current torch stream of the current device (read directly, without
+    the device-index resolution of torch.cuda.current_stream())."""
     override = getattr(_tls, "stream", None)
     if override is not None:
         return override
+    if _raw_stream is not None and _get_device is not None:
+        return int(_raw_stream(_get_device()))
     return int(torch.cuda.current_stream().cuda_stream)
 
 

@@ -161,6 +161,9 @@ def map(func=None, return_type=None, input_types=None):  # noqa: A001 - mirrors 
     return MappingFunction(func, return_type, input_types)
 
 
+_partial_counts: dict = {}  # n -> partial sums of the first stage (vdx_reduce_partial_count)
+
+
 class ReduceFunction:
     def __init__(self, reduction: ReduceOp, group_size: Optional[int] = None, axes: Optional[List[int]] = None,
                  mapping_function: Optional[MappingFunction] = None):
@@ -208,9 +211,12 @@ class ReduceFunction:
             out_code, out_type = L.VDX_F32, dt.float32
         if self.out_type is not None and self.out_type != out_type:
             raise NotImplementedError(f"map return type {self.out_type} does not match the reduction type {out_type}")
-        parts = ctypes.c_int64()
-        L.check(L.lib().vdx_reduce_partial_count(n, ctypes.byref(parts)), "reduce")
-        shape = (int(parts.value) + 1,) + ((batch,) if batch > 1 else ())
+        nparts = _partial_counts.get(n)
+        if nparts is None:
+            parts = ctypes.c_int64()
+            L.check(L.lib().vdx_reduce_partial_count(n, ctypes.byref(parts)), "reduce")
+            nparts = _partial_counts[n] = int(parts.value)
+        shape = (nparts + 1,) + ((batch,) if batch > 1 else ())
         res = Buffer(shape, out_type)
         op = self.reduction.code
         in_code = in_type.vdx_code
