@@ -68,20 +68,21 @@ struct TcLayout {
   static constexpr int TMEM_COLS = cmax(32, cmax(T1 * 32, T2 * 16));
 };
 
-// Stage-1 DFT vector of GEMM row v: (q, column).  For 32-column tiles the
-// low 3 bits of v pick the column within a group of 8 and the next 2 bits the
-// low bits of q, so a warp's 32 rows cover 8 columns x 4 values of q: its
-// stage-2 operand writes (row k1 * MT + column, K position 2q) fall in 32
-// distinct banks (row-major rows: 4-way conflicts, 13.1 M per launch -> 0.58 M)
-// and its tile loads are 4 rows x 8 columns of 4-byte values, whole 32-byte
-// sectors.  16-column tiles (8-byte storage) keep the row-major order: 2-way
-// conflicts there, and 128-byte row loads, measured faster.
-template <int MT>
+// Stage-1 DFT vector of GEMM row v: (q, column).  For 32-column tiles of
+// 4-byte storage the low 3 bits of v pick the column within a group of 8 and
+// the next 2 bits the low bits of q, so a warp's 32 rows cover 8 columns x 4
+// values of q: its stage-2 operand writes (row k1 * MT + column, K position
+// 2q) fall in 32 distinct banks (row-major rows: 4-way conflicts, 13.1 M per
+// launch -> 0.58 M) and its tile loads are 4 rows x 8 columns, whole 32-byte
+// sectors.  16-column tiles (the default) keep the row-major order, which
+// measured faster there (2-way conflicts, longer row segments).
+template <int MT, int ES>
 __device__ __forceinline__ void vec_qc(int v, int& q, int& c) {
-  if constexpr (MT == 32) {
+  if constexpr (ES == 4 && MT == 32) {
+    constexpr int CH = MT / 8;  // column groups of 8
     const int hi = v >> 5;
-    q = ((v >> 3) & 3) + 4 * (hi / 4);
-    c = (v & 7) + 8 * (hi % 4);
+    q = ((v >> 3) & 3) + 4 * (hi / CH);
+    c = (v & 7) + 8 * (hi % CH);
   } else {
     q = v / MT;
     c = v % MT;
@@ -117,7 +118,7 @@ __global__ void __launch_bounds__(kTcThreads) k_fs_tc(FsArgs a, const unsigned c
   for (int t = 0; t < Lay::T1; ++t) {
     const int v = t * 128 + tid;
     int q, c;
-    vec_qc<MT>(v, q, c);
+    vec_qc<MT, (int)sizeof(S)>(v, q, c);
     const int col = tile * MT + c;
     const bool valid = col < a.ncols;
     uint32_t hi[16], lo[16];
@@ -168,7 +169,7 @@ __global__ void __launch_bounds__(kTcThreads) k_fs_tc(FsArgs a, const unsigned c
     for (int t = 0; t < Lay::T1; ++t) {
       const int v = t * 128 + tid;
       int q, c;
-      vec_qc<MT>(v, q, c);
+      vec_qc<MT, (int)sizeof(S)>(v, q, c);
       float y[32];
       tc::tmem_ld16(lane_base + 32 * t, y);
       tc::tmem_ld16(lane_base + 32 * t + 16, y + 16);

@@ -272,7 +272,14 @@ int plan_fourstep(vdx_plan* p, long long inner, long long outer, int smem_optin)
     return fail(VDX_ERR_UNSUPPORTED, "FFT length " + std::to_string(N) + " has no four-step split into two lengths "
                                      "in [8, 4096]");
   const size_t sb = store_bytes(p->store);
-  const int mw = int(128 / sb);  // columns per tile: 128-byte row segments
+  int mw = int(128 / sb);  // columns per tile: 128-byte row segments
+  // tensor-core passes: 16 columns for every storage type (half the operand and
+  // staging shared memory of 32, so more CTAs per SM: 16384^2 bf16 3.68 ->
+  // 3.59 ms, fp16 3.76 -> 3.55 ms); VDX_TC_COLUMNS=32 restores 32 for 4-byte types
+  if (p->tensor_core) {
+    mw = 16;
+    if (const char* e = std::getenv("VDX_TC_COLUMNS")) mw = std::atoi(e) == 32 && sb == 4 ? 32 : 16;
+  }
   std::string why;
   auto tile_m = [&](int n, long long cols, int T) {
     int M = (int)std::min<long long>(mw, cols);
