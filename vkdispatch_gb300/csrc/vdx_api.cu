@@ -272,7 +272,12 @@ int plan_fourstep(vdx_plan* p, long long inner, long long outer, int smem_optin)
     return fail(VDX_ERR_UNSUPPORTED, "FFT length " + std::to_string(N) + " has no four-step split into two lengths "
                                      "in [8, 4096]");
   const size_t sb = store_bytes(p->store);
-  int mw = int(128 / sb);  // columns per tile: 128-byte row segments
+  // columns per tile: 32 on strided axes and 16 on contiguous ones, for every
+  // storage type (16384^2: strided c64 1.40 / 1.36 / 1.40 ms and bf16 1.20 /
+  // 1.13 / 1.19 ms at 16 / 32 / 64 columns; contiguous c64 1.56 / 1.70 / 1.70
+  // and bf16 1.41 / 1.49 / 1.60 ms); VDX_FS_COLUMNS overrides
+  int mw = inner > 1 ? 32 : 16;
+  if (const char* e = std::getenv("VDX_FS_COLUMNS")) mw = std::max(8, std::min(64, std::atoi(e)));
   // tensor-core passes: 16 columns for every storage type (half the operand and
   // staging shared memory of 32, so more CTAs per SM: 16384^2 bf16 3.68 ->
   // 3.59 ms, fp16 3.76 -> 3.55 ms); VDX_TC_COLUMNS=32 restores 32 for 4-byte types
