@@ -314,6 +314,8 @@ def _run_ours(args):
 
     extra = cfg1_numbers(vd, torch, flush, args) if rank == 0 and not args.quick else {}
     if rank == 0 and not args.quick:
+        extra["cfg2_rfft2_irfft2_roundtrip"] = roundtrip_numbers(vd, torch, flush, images)
+    if rank == 0 and not args.quick:
         extra["cfg3_diff_conv3d_256"] = cfg3_numbers(torch, flush)
         extra["cfg4_batched_uneven"] = cfg4_numbers(torch)
         extra["cfg5_mixed_precision_2d_16384"] = cfg5_numbers(torch)
@@ -454,6 +456,37 @@ def cfg1_numbers(vd, torch, flush, args):
     out["cfg1_hbm_1024x262144"] = res
     del big
     return out
+
+
+def roundtrip_numbers(vd, torch, flush, images, steps=20):
+    """The rfft2 -> irfft2 round trip of the Cfg2 images (64 x 512x512 f32):
+    rfft of the rows, FFT of the 257 spectrum columns, inverse, irfft of the
+    rows.  Algorithmic bytes: each of the 4 passes reads and writes its array
+    once (real rows 64 MiB, half spectrum 67,371,008 B)."""
+    buf = vd.RFFTBuffer((B, H, W))
+    buf.write_real(images)
+    vd.fft.rfft2(buf)
+    spec = buf.read_fourier(0)
+    ref = np.fft.rfft2(images.astype(np.float64))
+    spec_err = float(np.linalg.norm(spec - ref) / np.linalg.norm(ref))
+    vd.fft.irfft2(buf)
+    rt_err = float(np.linalg.norm(buf.read_real(0) - images) / np.linalg.norm(images))
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ts = []
+    for _ in range(steps):
+        flush.zero_()
+        ev[0].record()
+        vd.fft.rfft2(buf)
+        vd.fft.irfft2(buf)
+        ev[1].record()
+        torch.cuda.synchronize()
+        ts.append(ev[0].elapsed_time(ev[1]))
+    ms = statistics.median(ts)
+    alg = 2 * (REAL_BYTES + SPEC_BYTES) + 4 * SPEC_BYTES
+    peak, _ = _load_peaks()
+    return {"ms": round(ms, 4), "algorithmic_bytes": alg, "GBps": round(alg / (ms * 1e-3) / 1e9, 1),
+            "frac_of_measured_hbm": round(alg / (ms * 1e-3) / 1e9 / peak, 4), "launches": 4,
+            "rfft2_rel_l2_vs_fp64": spec_err, "roundtrip_rel_l2": rt_err}
 
 
 def cfg3_numbers(torch, flush, steps=10):
