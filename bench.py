@@ -589,7 +589,7 @@ def cfg4_numbers(torch, reps=10):
     g = torch.Generator(device="cuda").manual_seed(3)
     data = torch.randn(points, dtype=torch.complex64, device="cuda", generator=g)
     x0 = data.clone()
-    plan = BatchPlan(items)
+    plan = BatchPlan(items, autotune=True)  # CTA size timed on scratch buffers at creation
     desc = plan.describe()
     ws = plan.make_workspace()
     long_points = desc["long_points"]
@@ -667,7 +667,7 @@ def cfg4_numbers(torch, reps=10):
     torch.cuda.empty_cache()
     return {
         "items": len(items), "distinct_lengths": len(set(lengths)), "seven_smooth_sizes_in_range": nsmooth,
-        "points": points, "long_points": long_points, "plan": desc,
+        "points": points, "long_points": long_points, "plan": desc, "autotuned_cta_threads": plan.cta,
         "algorithmic_bytes": bytes_alg,
         "persistent_graph_ms": round(t_persist, 4),
         "persistent_GBps": round(bytes_alg / (t_persist * 1e-3) / 1e9, 1),

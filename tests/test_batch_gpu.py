@@ -87,3 +87,26 @@ def test_bad_items_rejected():
         BatchPlan([(0, 17 * 4099, 1)])  # prime factor above 13
     with pytest.raises(ValueError):
         BatchPlan([(0, 0, 1)])
+
+
+def test_autotuned_batch_plan_matches_numpy():
+    """BatchPlan(autotune=True) picks a CTA size by timing; results stay within the bound."""
+    import torch
+    from vkdispatch_gb300.batch import BatchPlan, pack_items
+
+    rng = np.random.default_rng(44)
+    lengths = [16, 48, 625, 1024, 2187, 9604, 40000]
+    items, total = pack_items((n, max(1, 60000 // n)) for n in lengths)
+    x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex64)
+    t = torch.from_numpy(x).cuda()
+    plan = BatchPlan(items, autotune=True)
+    assert plan.cta in (256, 512, 1024)
+    ws = plan.make_workspace()
+    plan(t, ws)
+    torch.cuda.synchronize()
+    got = t.cpu().numpy()
+    for off, n, c in items:
+        ref = np.fft.fft(x[off:off + n * c].reshape(c, n).astype(np.complex128), axis=1)
+        err = np.linalg.norm(got[off:off + n * c].reshape(c, n) - ref) / np.linalg.norm(ref)
+        assert err <= 5e-7 * max(1.0, np.log2(n)) * 2
+    assert plan.status() == 0
