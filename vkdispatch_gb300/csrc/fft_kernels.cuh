@@ -543,10 +543,12 @@ __global__ void __launch_bounds__(1024) k_conv(FftArgs a) {
   store_output<Plan, true, S, Re>(P, pl, a, v);
 }
 
-// Strided fused convolution for CTAs of at most 256 threads: the kernel
-// spectrum is loaded into registers before the forward FFT, so its HBM
-// latency overlaps the forward passes instead of following them (the
-// registers it takes need the 256-thread launch bound).
+// Strided fused convolution for CTAs of at most 256 threads (complex64).
+// The signal loads are issued first and the kernel-spectrum loads right
+// after them, into registers, so the kernel spectrum's HBM latency overlaps
+// the forward passes instead of following them (the registers it takes need
+// the 256-thread launch bound).  The kernel spectrum is read once, with
+// evict-first loads.
 template <class Plan, class S, class Re, int KOP>
 __global__ void __launch_bounds__(256) k_conv_pf(FftArgs a) {
   const Plan P(a.pp);
@@ -559,6 +561,8 @@ __global__ void __launch_bounds__(256) k_conv_pf(FftArgs a) {
   P.assume_t(pl.t);
   const int n = P.n();
   const bool kvalid = pl.tile_full || pl.valid;
+  Cx<Re> v[MAXE];
+  gather_input<Plan, S, Re>(P, pl, a, v, in);
   Cx<Re> kr[MAXE];
   P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
@@ -569,11 +573,9 @@ __global__ void __launch_bounds__(256) k_conv_pf(FftArgs a) {
       const int j = pl.t + b * P.T();
 #pragma unroll
       for (int r = 0; r < RR; ++r)
-        kr[b * RR + r] = (j < nb && kvalid) ? Conv<S, Re>::ld(ker + (j + r * nb) * pl.ps) : mk<Re>(Re(0), Re(0));
+        kr[b * RR + r] = (j < nb && kvalid) ? ld_once<S, Re>(ker + (j + r * nb) * pl.ps) : mk<Re>(Re(0), Re(0));
     }
   });
-  Cx<Re> v[MAXE];
-  gather_input<Plan, S, Re>(P, pl, a, v, in);
   P.template run<false, false>(v, pl, sm, tw);
   P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;

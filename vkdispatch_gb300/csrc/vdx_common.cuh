@@ -399,4 +399,15 @@ __device__ __forceinline__ void st_real(__half* p, Re v) { *p = __float2half_rn(
 template <class Re>
 __device__ __forceinline__ void st_real(__nv_bfloat16* p, Re v) { *p = __float2bfloat16_rn(float(v)); }
 
+// read-once load marked evict-first (ld.global.cs for complex64): a kernel
+// spectrum read once per launch leaves room in L2 for the outputs that the
+// next launch reads
+template <class S, class Re>
+__device__ __forceinline__ Cx<Re> ld_once(const S* p) { return Conv<S, Re>::ld(p); }
+template <>
+__device__ __forceinline__ Cx<float> ld_once<Cx<float>, float>(const Cx<float>* p) {
+  const float2 f = __ldcs(reinterpret_cast<const float2*>(p));
+  return mk<float>(f.x, f.y);
+}
+
 }  // namespace vdx
