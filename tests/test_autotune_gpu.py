@@ -61,6 +61,6 @@ def test_cache_hits_and_round_trip(tmp_path):
     path = tmp_path / "tune.txt"
     vd.fft.autotune_save(path)
     lines = [ln for ln in path.read_text().splitlines() if not ln.startswith("#")]
-    assert len(lines) == entries and all(len(ln.split()) == 16 for ln in lines)
+    assert len(lines) == entries and all(len(ln.split()) == 17 for ln in lines)
     vd.fft.autotune_load(path)
     assert vd.fft.autotune_stats()[0] == entries

@@ -290,3 +290,31 @@ def test_from_cuda_array_checks():
         vd.from_cuda_array(t.t())  # non-contiguous
     with pytest.raises(ValueError):
         vd.from_cuda_array(t, var_type=vd.complex128)
+
+
+@pytest.mark.parametrize("kop_conj", [True, False])
+def test_strided_convolution_eight_points_per_thread(monkeypatch, kop_conj):
+    """The radix-8 compile-time plan (64 threads per 512-point column) of the
+    strided fused convolution matches FP64 numpy, conjugate and plain product."""
+    import torch
+
+    from vkdispatch_gb300 import _lib as L
+    from vkdispatch_gb300.fft import plan as P
+
+    monkeypatch.setenv("VDX_CONV_POINTS_PER_THREAD", "8")
+    P.cache_clear()
+    rng = np.random.default_rng(31 + kop_conj)
+    shape = (3, 512, 257)
+    x = crandn(rng, shape)
+    k = crandn(rng, shape)
+    xt, kt = torch.from_numpy(x).cuda(), torch.from_numpy(k).cuda()
+    kop = L.VDX_KOP_MUL_CONJ if kop_conj else L.VDX_KOP_MUL
+    p = P.get_plan(shape, 1, L.VDX_KIND_CONV, False, True, L.VDX_C64, L.VDX_C64, None, kop, L.VDX_C64)
+    d = p.describe()
+    assert d["threads_per_transform"] == 64 and d["radices"] == "8x8x8" and d["fixed"] is True
+    p.exec(xt.data_ptr(), xt.data_ptr(), kt.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    s = np.fft.fft(x.astype(np.complex128), axis=1)
+    ref = np.fft.ifft(s * (np.conj(k) if kop_conj else k), axis=1)
+    assert rel_l2(xt.cpu().numpy(), ref) <= 2 * tol_fp32(512)
+    P.cache_clear()

@@ -25,4 +25,13 @@ cudaError_t launch_fixed_c64_any(int n, const FftArgs& a, const Launch& l, int o
   }
 }
 
+bool has_fixed8_conv_c64(int n) { return n == 512; }
+
+cudaError_t launch_fixed8_conv_c64_any(int n, const FftArgs& a, const Launch& l, int kop, int variant) {
+  switch (n) {
+    case 512: return launch_fixed8_conv_c64<512>(a, l, kop, variant);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 }  // namespace vdx

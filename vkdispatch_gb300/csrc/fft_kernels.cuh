@@ -543,14 +543,15 @@ __global__ void __launch_bounds__(1024) k_conv(FftArgs a) {
   store_output<Plan, true, S, Re>(P, pl, a, v);
 }
 
-// Strided fused convolution for CTAs of at most 256 threads (complex64).
+// Strided fused convolution for CTAs of at most 256 threads, complex64 (two
+// CTAs per SM with 16 points per thread, three with 8).
 // The signal loads are issued first and the kernel-spectrum loads right
 // after them, into registers, so the kernel spectrum's HBM latency overlaps
 // the forward passes instead of following them (the registers it takes need
 // the 256-thread launch bound).  The kernel spectrum is read once, with
 // evict-first loads.
 template <class Plan, class S, class Re, int KOP>
-__global__ void __launch_bounds__(256) k_conv_pf(FftArgs a) {
+__global__ void __launch_bounds__(256, Plan::MAXE <= 8 ? 3 : 2) k_conv_pf(FftArgs a) {
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
   const Place<true> pl(a, P.T());
@@ -796,6 +797,16 @@ template <> struct Pow2<16384> { using L = RList<16, 16, 16, 4>; static constexp
 
 template <int N>
 using Pow2Plan = FixPlan<N, Pow2<N>::T, typename Pow2<N>::L>;
+
+// compile-time plans of radix-8 passes, 8 points per thread (n/8 threads per
+// transform): half the registers of the radix-16 plans, for the strided
+// fused convolution that also holds the kernel spectrum in registers
+template <int N>
+struct Pow2x8;
+template <> struct Pow2x8<512> { using L = RList<8, 8, 8>; static constexpr int T = 64; };
+
+template <int N>
+using Pow2x8Plan = FixPlan<N, Pow2x8<N>::T, typename Pow2x8<N>::L, 8>;
 
 
 }  // namespace vdx

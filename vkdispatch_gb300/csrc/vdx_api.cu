@@ -181,6 +181,7 @@ struct Tune {
   int order = 0;      // radix passes: 0 = largest radix first, 1 = smallest first
   int fixed = -1;     // compile-time kernels where available: -1 = yes, 0 = no
   int fourstep = -1;  // long C2C axes: -1 = from 8192 points (VDX_FOURSTEP_MIN), 0 = only above one CTA, 1 = always
+  int maxe = 16;      // points per thread: 16, or 8 (strided complex64 convolutions with a compile-time plan)
 };
 }  // namespace vdx
 
@@ -200,6 +201,7 @@ struct vdx_plan {
   // `chunk_cols` columns x `chunk_outer` outer batches (strided axes) or
   // `chunk_outer` rows (contiguous axes); `ws` holds one chunk
   bool fourstep = false;
+  bool fixed8 = false;  // strided convolution on the 8-points-per-thread compile-time plan
   int N1 = 0, N0 = 0;
   long long inner = 1, outer = 1;
   long long chunk_cols = 0, chunk_outer = 0;
@@ -696,7 +698,18 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
 
   const bool even_real = real && (N % 2 == 0);
   const int n = even_real ? N / 2 : N;  // complex points per transform
-  const int maxe = f64 ? MaxE<double>::value : MaxE<float>::value;
+  // 8 points per thread: strided complex64 convolutions with a compile-time
+  // plan, chosen by the autotuner or by VDX_CONV_POINTS_PER_THREAD=8
+  const bool can8 = d.kind == VDX_KIND_CONV && inner > 1 && st == ST_C64 && !f64 && has_fixed8_conv_c64(N) &&
+                    tune.order == 0 && tune.fixed != 0 && std::getenv("VDX_NO_FIXED") == nullptr;
+  int pmaxe = tune.maxe == 8 ? 8 : 16;
+  if (const char* e = std::getenv("VDX_CONV_POINTS_PER_THREAD"))
+    if (std::atoi(e) == 8 && can8) pmaxe = 8;
+  if (pmaxe == 8 && !can8) {
+    delete p;
+    return fail(VDX_ERR_UNSUPPORTED, "8 points per thread exist for strided complex64 convolutions of 512 points");
+  }
+  const int maxe = f64 ? MaxE<double>::value : (pmaxe == 8 ? 8 : MaxE<float>::value);
   std::string why;
   if (!factor_radices(n, maxe, p->radices, why)) {
     delete p;
@@ -849,6 +862,11 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
   p->fixed = st == ST_C64 && !f64 && has_fixed_c64(n) && p->op != OP_R2C_ODD &&
              p->op != OP_C2R_ODD && T == n / 16 && std::getenv("VDX_NO_FIXED") == nullptr && tune.order == 0 &&
              tune.fixed != 0;
+  p->fixed8 = pmaxe == 8 && T == n / 8 && p->op == OP_CONV && strided;
+  if (pmaxe == 8 && !p->fixed8) {
+    delete p;
+    return fail(VDX_ERR_UNSUPPORTED, "no compile-time plan of 8 points per thread for this convolution");
+  }
 
   void* tw = nullptr;
   int rc = get_table(p->dev, n, n, f64, &tw);
@@ -1015,6 +1033,14 @@ int autotune_plan(const vdx_fft_desc& d0, vdx_plan** plan) {
             t.fourstep = fsv;
             cands.push_back(t);
           }
+    // strided complex64 convolutions: the 8-points-per-thread compile-time plan
+    if (d.kind == VDX_KIND_CONV && inner_t > 1 && d.io_type == VDX_C64 && d.compute_type == VDX_C64)
+      for (int w : widths) {
+        Tune t;
+        t.width = w;
+        t.maxe = 8;
+        cands.push_back(t);
+      }
     std::vector<std::string> seen;
     for (const Tune& t : cands) {
       vdx_plan* c = nullptr;
@@ -1100,10 +1126,11 @@ int vdx_autotune_save(const char* path) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
   FILE* f = std::fopen(path, "w");
   if (!f) return fail(VDX_ERR_INVALID, std::string("cannot write ") + path);
-  std::fprintf(f, "# libvdx autotune cache: 12 key fields, then width order fixed fourstep\n");
+  std::fprintf(f, "# libvdx autotune cache: 12 key fields, then width order fixed fourstep points-per-thread\n");
   for (const auto& kv : g_tuned) {
     for (int v : kv.first) std::fprintf(f, "%d ", v);
-    std::fprintf(f, "%d %d %d %d\n", kv.second.width, kv.second.order, kv.second.fixed, kv.second.fourstep);
+    std::fprintf(f, "%d %d %d %d %d\n", kv.second.width, kv.second.order, kv.second.fixed, kv.second.fourstep,
+                 kv.second.maxe);
   }
   std::fclose(f);
   return VDX_OK;
@@ -1120,15 +1147,18 @@ int vdx_autotune_load(const char* path) {
     if (line[0] == '#') continue;
     TuneKey k{};
     Tune t;
-    int v[16];
-    int cnt = std::sscanf(line, "%d %d %d %d %d %d %d %d %d %d %d %d %d %d %d %d", &v[0], &v[1], &v[2], &v[3], &v[4],
-                          &v[5], &v[6], &v[7], &v[8], &v[9], &v[10], &v[11], &v[12], &v[13], &v[14], &v[15]);
-    if (cnt != 16) continue;
+    int v[17];
+    v[16] = 16;  // caches written before the points-per-thread field hold 16
+    int cnt = std::sscanf(line, "%d %d %d %d %d %d %d %d %d %d %d %d %d %d %d %d %d", &v[0], &v[1], &v[2], &v[3],
+                          &v[4], &v[5], &v[6], &v[7], &v[8], &v[9], &v[10], &v[11], &v[12], &v[13], &v[14], &v[15],
+                          &v[16]);
+    if (cnt != 16 && cnt != 17) continue;
     for (int i = 0; i < 12; ++i) k[i] = v[i];
     t.width = v[12];
     t.order = v[13];
     t.fixed = v[14];
     t.fourstep = v[15];
+    t.maxe = v[16] == 8 ? 8 : 16;
     g_tuned[k] = t;
     ++loaded;
   }
@@ -1174,11 +1204,11 @@ int vdx_fft_plan_describe(const vdx_plan* p, char* buf, size_t n) {
   std::snprintf(buf, n,
                 "{\"op\": \"%s\", \"N\": %d, \"n\": %d, \"radices\": \"%s\", \"threads_per_transform\": %d, "
                 "\"transforms_per_cta\": %d, \"strided\": %s, \"fixed\": %s, \"grid\": %u, \"block\": %u, "
-                "\"smem\": %zu, \"autotuned\": %s, \"tune\": [%d, %d, %d, %d], \"tune_candidates\": %d}",
+                "\"smem\": %zu, \"autotuned\": %s, \"tune\": [%d, %d, %d, %d, %d], \"tune_candidates\": %d}",
                 ops[p->op], p->N, p->args.pp.n, r.c_str(), p->args.pp.T, p->args.pp.M, p->strided ? "true" : "false",
-                p->fixed ? "true" : "false", p->launch.grid.x, p->launch.block.x, p->launch.smem,
+                (p->fixed || p->fixed8) ? "true" : "false", p->launch.grid.x, p->launch.block.x, p->launch.smem,
                 p->tuned ? "true" : "false", p->tune.width, p->tune.order, p->tune.fixed, p->tune.fourstep,
-                p->tuned_candidates);
+                p->tune.maxe, p->tuned_candidates);
   return VDX_OK;
 }
 
@@ -1261,6 +1291,11 @@ int exec_plan(const vdx_plan* p, const void* in, void* out, const void* kernel, 
   }
   Launch l = p->launch;
   l.stream = reinterpret_cast<cudaStream_t>(stream);
+  if (p->fixed8) {
+    e = launch_fixed8_conv_c64_any(p->args.pp.n, a, l, p->d.kernel_op, variant);
+    if (e != cudaSuccess) return cuda_fail(e, "FFT launch");
+    return VDX_OK;
+  }
   if (p->fixed) {
     e = launch_fixed_c64_any(p->args.pp.n, a, l, p->op, p->strided, p->d.kernel_op, variant);
     if (e != cudaSuccess) return cuda_fail(e, "FFT launch");

@@ -115,6 +115,12 @@ cudaError_t launch_fixed_c64(const FftArgs& a, const Launch& l, int op, bool str
 bool has_fixed_c64(int n);
 cudaError_t launch_fixed_c64_any(int n, const FftArgs& a, const Launch& l, int op, bool strided, int kop,
                                  int variant);
+// strided complex64 convolution, radix-8 passes with n/8 threads per
+// transform (n = 512)
+template <int N>
+cudaError_t launch_fixed8_conv_c64(const FftArgs& a, const Launch& l, int kop, int variant);
+bool has_fixed8_conv_c64(int n);
+cudaError_t launch_fixed8_conv_c64_any(int n, const FftArgs& a, const Launch& l, int kop, int variant);
 
 // Opt a kernel into more than 48 KB of dynamic shared memory once.
 template <class K>
