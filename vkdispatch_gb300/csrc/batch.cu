@@ -45,6 +45,8 @@ struct UnitPlan {
 };
 
 struct WorkUnit {
+  PassPlan pp;                  // the unit's pass plan (a copy, so one table read fetches everything)
+  const Cx<float>* tw;          // W_n^k for the unit's transform length
   long long src, dst;           // element offset of point 0 of slot 0 (data or workspace)
   long long src_slot, dst_slot;  // elements between slots
   long long src_pt, dst_pt;     // elements between points
@@ -91,10 +93,13 @@ struct UnitPlace {
 // between items.
 template <bool INV>
 __device__ __forceinline__ void run_unit(const BatchArgs& a, const WorkUnit* __restrict__ pu, int kind,
-                                         const PassPlan& pp, Cx<float>* sm) {
+                                         Cx<float>* sm) {
   constexpr int MAXE = 16;
-  const WorkUnit& wu = *pu;  // fields are read from the (L1-cached, CTA-uniform) unit table
-  const Cx<float>* tw = a.plans[wu.plan].tw;
+  // fields are read from the (L1-cached, CTA-uniform) unit table: read-only
+  // global loads the compiler may repeat instead of holding them in registers
+  const WorkUnit& wu = *pu;
+  const PassPlan& pp = wu.pp;
+  const Cx<float>* tw = wu.tw;
   const int n = pp.n, T = pp.T, M = pp.M;
   const bool cols = kind == UK_COLS;
   UnitPlace pl;
@@ -144,36 +149,49 @@ __device__ __forceinline__ void run_unit(const BatchArgs& a, const WorkUnit* __r
   });
 }
 
-// THREADS per CTA, MINB resident CTAs per SM (64 registers per thread)
+// THREADS per CTA, MINB resident CTAs per SM (64 registers per thread).
+//
+// Claiming runs two units ahead: while a CTA works on unit u it already
+// knows the next unit, whose descriptor (pass plan included) is prefetched
+// into L1 at the start of u, and thread 0 holds the ticket of the one after,
+// whose atomic was issued a whole unit earlier.  No ticket or pass-plan
+// round trip to L2 lies between two units.  A CTA may hold two claimed
+// units, but a claimed UK_COLS unit only ever follows another UK_COLS unit
+// of the same CTA, which does not wait, so every claimed UK_COLS unit runs.
+constexpr int kUnitLines = int((sizeof(WorkUnit) + 127) / 128) + 1;  // 128-byte lines a descriptor touches
+
 template <bool INV, int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_batch(BatchArgs a) {
-  __shared__ int s_unit;
-  __shared__ int s_next;
+  // (current, next) unit indices, double-buffered by iteration parity so
+  // that one barrier per unit separates their reads from the next writes
+  __shared__ int s_cur[2], s_next[2];
   __shared__ int s_ok;
-  __shared__ PassPlan s_pp;  // the current unit's pass plan
   Cx<float>* sm = smem_base<float>();
-  if (threadIdx.x == 0) s_next = (int)atomicAdd(a.ticket, 1u);
-  for (;;) {
-    __syncthreads();
-    // take the unit claimed during the previous one and claim the next now,
-    // so the ticket's round trip overlaps this unit's work
-    if (threadIdx.x == 0) {
-      s_unit = s_next;
-      if (s_next < a.nunits) s_next = (int)atomicAdd(a.ticket, 1u);
-    }
-    __syncthreads();
-    const int u = s_unit;
+  const int tid = threadIdx.x;
+  int claim = 0;  // thread 0: the ticket two units ahead
+  if (tid == 0) {
+    s_cur[0] = (int)atomicAdd(a.ticket, 1u);
+    s_next[0] = (int)atomicAdd(a.ticket, 1u);
+    claim = s_next[0] < a.nunits ? (int)atomicAdd(a.ticket, 1u) : a.nunits;
+  }
+  __syncthreads();
+  for (int par = 0;; par ^= 1) {
+    const int u = s_cur[par];
     if (u >= a.nunits) return;
+    const int un = s_next[par];
+    if (tid < kUnitLines && un < a.nunits) {
+      const char* line = reinterpret_cast<const char*>(&a.units[un]) + 128 * tid;
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(line));
+    }
     const WorkUnit* pu = &a.units[u];
-    const int kind = pu->kind;
-    if (threadIdx.x < (int)(sizeof(PassPlan) / sizeof(int)))
-      reinterpret_cast<int*>(&s_pp)[threadIdx.x] = reinterpret_cast<const int*>(&a.plans[pu->plan].pp)[threadIdx.x];
-    __syncthreads();
+    const WorkUnit& wu = *pu;
+    const int kind = wu.kind;
+    bool run = true;
     if (kind == UK_ROWS2) {
-      if (threadIdx.x == 0) {
+      if (tid == 0) {
         int ok = 1;
         long long polls = 0;
-        const int item = pu->item, wait = pu->wait;
+        const int item = wu.item, wait = wu.wait;
         while (atomicAdd(&a.counters[item], 0) < wait) {
           if (++polls > kWaitLimit) {
             atomicExch(a.status, 1);
@@ -186,14 +204,22 @@ __global__ void __launch_bounds__(THREADS, MINB) k_batch(BatchArgs a) {
         s_ok = ok;
       }
       __syncthreads();
-      if (!s_ok) continue;
+      run = s_ok != 0;
     }
-    run_unit<INV>(a, pu, kind, s_pp, sm);
+    if (run) run_unit<INV>(a, pu, kind, sm);
     if (kind == UK_COLS) {
       __threadfence();
       __syncthreads();
-      if (threadIdx.x == 0) atomicAdd(&a.counters[pu->item], 1);
+      if (tid == 0) atomicAdd(&a.counters[wu.item], 1);
     }
+    // move the ticket pipeline on by one; the barrier also keeps the next
+    // unit's shared-memory exchanges clear of this unit's last reads
+    if (tid == 0) {
+      s_cur[par ^ 1] = un;
+      s_next[par ^ 1] = claim;
+      if (claim < a.nunits) claim = (int)atomicAdd(a.ticket, 1u);
+    }
+    __syncthreads();
   }
 }
 
@@ -351,6 +377,8 @@ int vdx_batch_plan_create(const vdx_batch_item* items, int nitems, int inverse, 
         WorkUnit w{};
         w.kind = UK_ROWS;
         w.plan = p;
+        w.pp = plans[p].pp;
+        w.tw = plans[p].tw;
         w.src = w.dst = it.offset + t0 * L;
         w.src_slot = w.dst_slot = L;
         w.src_pt = w.dst_pt = 1;
@@ -382,6 +410,8 @@ int vdx_batch_plan_create(const vdx_batch_item* items, int nitems, int inverse, 
         WorkUnit w{};
         w.kind = UK_COLS;
         w.plan = pc;
+        w.pp = plans[pc].pp;
+        w.tw = plans[pc].tw;
         w.src = it.offset + bt * L + c0;
         w.dst = wsoff + bt * L + c0;
         w.src_slot = w.dst_slot = 1;
@@ -400,6 +430,8 @@ int vdx_batch_plan_create(const vdx_batch_item* items, int nitems, int inverse, 
         WorkUnit w{};
         w.kind = UK_ROWS2;
         w.plan = pr;
+        w.pp = plans[pr].pp;
+        w.tw = plans[pr].tw;
         w.src = wsoff + bt * L + (long long)r0 * L2;
         w.dst = it.offset + bt * L + r0;
         w.src_slot = L2;
