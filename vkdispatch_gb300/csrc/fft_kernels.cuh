@@ -186,15 +186,29 @@ __device__ __forceinline__ void each_natural(Cx<Re>* v, int nb, int T, int t, F&
   }
 }
 
-template <int R, int MAXE, bool INV, class Re>
-__device__ __forceinline__ void butterflies(Cx<Re>* v, int nb, int T, int t, int ns, int n, const Cx<Re>* tw) {
+// j mod d for d >= 2 and j * d < 2^32, given m = ceil(2^32 / d): one
+// multiply-high and a multiply-subtract instead of an integer division by a
+// runtime value (division by invariant integers, Granlund & Montgomery,
+// PLDI 1994: with m = (2^32 + e) / d, 0 <= e < d, the floor of j m / 2^32 is
+// floor(j / d) while j e < 2^32).  Transform indices stay below 2^15, so
+// j * d < 2^30 for every pass of every supported length.
+__device__ __forceinline__ int mod_inv(int j, int d, unsigned m) {
+  return j - int(__umulhi(unsigned(j), m)) * d;
+}
+__host__ __device__ __forceinline__ unsigned inv_magic(int d) { return d > 1 ? 0xFFFFFFFFu / unsigned(d) + 1u : 0u; }
+
+// RT: ns is a runtime value with nsm = inv_magic(ns); otherwise ns is a
+// compile-time constant and j % ns folds
+template <int R, int MAXE, bool INV, class Re, bool RT = false>
+__device__ __forceinline__ void butterflies(Cx<Re>* v, int nb, int T, int t, int ns, int n, const Cx<Re>* tw,
+                                            unsigned nsm = 0) {
   constexpr int B = MAXE / R;
 #pragma unroll
   for (int b = 0; b < B; ++b) {
     const int j = t + b * T;
     if (j < nb) {
       if (ns > 1) {
-        const int k = j % ns;
+        const int k = RT ? mod_inv(j, ns, nsm) : j % ns;
         const int step = k * (n / (ns * R));
 #pragma unroll
         for (int r = 1; r < R; ++r) {
@@ -207,14 +221,14 @@ __device__ __forceinline__ void butterflies(Cx<Re>* v, int nb, int T, int t, int
   }
 }
 
-template <int R, int MAXE, class Re, class G>
-__device__ __forceinline__ void scatter(const Cx<Re>* v, int nb, int T, int t, int ns, G&& g) {
+template <int R, int MAXE, class Re, bool RT = false, class G>
+__device__ __forceinline__ void scatter(const Cx<Re>* v, int nb, int T, int t, int ns, G&& g, unsigned nsm = 0) {
   constexpr int B = MAXE / R;
 #pragma unroll
   for (int b = 0; b < B; ++b) {
     const int j = t + b * T;
     if (j < nb) {
-      const int k = j % ns;
+      const int k = RT ? (ns > 1 ? mod_inv(j, ns, nsm) : 0) : j % ns;
       const int base = (j - k) * R + k;
 #pragma unroll
       for (int r = 0; r < R; ++r) g(base + r * ns, v[b * R + r]);
@@ -234,13 +248,15 @@ __device__ __forceinline__ void run_passes(Cx<Re>* v, const PassPlan& pp, bool r
     const int p = reversed ? P - 1 - q : q;
     const int R = pp.radix[p];
     const bool more = q + 1 < P;
+    const unsigned nsm = inv_magic(ns);  // one division per pass instead of one per butterfly index
     // one radix dispatch per pass covers the butterflies and the scatter
     radix_dispatch(R, [&](auto rc) {
       constexpr int RR = decltype(rc)::value;
-      butterflies<RR, MAXE, INV, Re>(v, n / RR, T, t, ns, n, tw);
+      butterflies<RR, MAXE, INV, Re, true>(v, n / RR, T, t, ns, n, tw, nsm);
       if (more) {
         xsync(warp);
-        scatter<RR, MAXE, Re>(v, n / RR, T, t, ns, [&](int pos, Cx<Re> val) { sm[pl.sidx(pp, pos)] = val; });
+        scatter<RR, MAXE, Re, true>(
+            v, n / RR, T, t, ns, [&](int pos, Cx<Re> val) { sm[pl.sidx(pp, pos)] = val; }, nsm);
       }
     });
     if (more) {
