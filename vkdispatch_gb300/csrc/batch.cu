@@ -121,7 +121,8 @@ __device__ __forceinline__ void run_unit(const BatchArgs& a, const WorkUnit* __r
   if (!active) pl.t = 1 << 20;  // every butterfly index of an idle thread is out of range
   const bool valid = active && pl.m < wu.nslots;
   const Cx<float>* src = (kind == UK_ROWS2 ? a.ws : a.data) + wu.src + pl.m * wu.src_slot;
-  const long long src_pt = wu.src_pt;
+  // point offsets inside a unit stay below 2^28 (n, L1, L2 <= 16384): 32-bit
+  const int src_pt = int(wu.src_pt);
   Cx<float> v[MAXE];
   radix_dispatch(pp.radix[0], [&](auto rc) {
     constexpr int RR = decltype(rc)::value;
@@ -133,17 +134,17 @@ __device__ __forceinline__ void run_unit(const BatchArgs& a, const WorkUnit* __r
   // row units keep each transform inside one warp when T divides 32
   run_passes<MAXE, INV>(v, pp, false, pl, sm, tw, !cols && warp_sized(T));
   Cx<float>* dst = (kind == UK_COLS ? a.ws : a.data) + wu.dst + pl.m * wu.dst_slot;
-  const long long dst_pt = wu.dst_pt;
+  const int dst_pt = int(wu.dst_pt);
   const bool twiddle = cols;
   const Cx<float> sc = mk<float>(wu.scale, 0.f);
-  const Cx<float>* twl = wu.twl + (twiddle ? (long long)(wu.c0 + pl.m) : 0);
-  const long long twstep = twiddle ? (long long)(wu.c0 + pl.m) : 0;
+  const Cx<float>* twl = wu.twl;
+  const int twstep = twiddle ? wu.c0 + pl.m : 0;  // n2; n2 * k1 < L <= 2^24
   radix_dispatch(pp.radix[pp.npass - 1], [&](auto rc) {
     constexpr int RR = decltype(rc)::value;
     each_natural<RR, MAXE, float>(v, n / RR, T, pl.t, [&](int pos, Cx<float> val) {
       if (!valid) return;
       // W_L^{n2 k1} with n2 = column, k1 = pos (n2 k1 < L), or the scale
-      const Cx<float> w = twiddle ? ldg(twl - twstep + twstep * pos) : sc;
+      const Cx<float> w = twiddle ? ldg(twl + twstep * pos) : sc;
       dst[pos * dst_pt] = INV ? cmulc(val, w) : cmul(val, w);
     });
   });

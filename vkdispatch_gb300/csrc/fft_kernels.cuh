@@ -197,11 +197,11 @@ __device__ __forceinline__ int mod_inv(int j, int d, unsigned m) {
 }
 __host__ __device__ __forceinline__ unsigned inv_magic(int d) { return d > 1 ? 0xFFFFFFFFu / unsigned(d) + 1u : 0u; }
 
-// RT: ns is a runtime value with nsm = inv_magic(ns); otherwise ns is a
-// compile-time constant and j % ns folds
+// RT: ns is a runtime value with nsm = inv_magic(ns) and tws = n / (ns R);
+// otherwise ns is a compile-time constant and j % ns folds
 template <int R, int MAXE, bool INV, class Re, bool RT = false>
 __device__ __forceinline__ void butterflies(Cx<Re>* v, int nb, int T, int t, int ns, int n, const Cx<Re>* tw,
-                                            unsigned nsm = 0) {
+                                            unsigned nsm = 0, int tws = 0) {
   constexpr int B = MAXE / R;
 #pragma unroll
   for (int b = 0; b < B; ++b) {
@@ -209,7 +209,7 @@ __device__ __forceinline__ void butterflies(Cx<Re>* v, int nb, int T, int t, int
     if (j < nb) {
       if (ns > 1) {
         const int k = RT ? mod_inv(j, ns, nsm) : j % ns;
-        const int step = k * (n / (ns * R));
+        const int step = k * (RT ? tws : n / (ns * R));
 #pragma unroll
         for (int r = 1; r < R; ++r) {
           const Cx<Re> w = ldg(&tw[r * step]);
@@ -249,10 +249,11 @@ __device__ __forceinline__ void run_passes(Cx<Re>* v, const PassPlan& pp, bool r
     const int R = pp.radix[p];
     const bool more = q + 1 < P;
     const unsigned nsm = inv_magic(ns);  // one division per pass instead of one per butterfly index
+    const int tws = n / (ns * R);       // twiddle stride of the pass
     // one radix dispatch per pass covers the butterflies and the scatter
     radix_dispatch(R, [&](auto rc) {
       constexpr int RR = decltype(rc)::value;
-      butterflies<RR, MAXE, INV, Re, true>(v, n / RR, T, t, ns, n, tw, nsm);
+      butterflies<RR, MAXE, INV, Re, true>(v, n / RR, T, t, ns, n, tw, nsm, tws);
       if (more) {
         xsync(warp);
         scatter<RR, MAXE, Re, true>(
