@@ -263,7 +263,7 @@ def _run_ours(args):
     dom = max(mean_k, key=mean_k.get)
     peak, peak_kind = _load_peaks()
     achieved = ALG_BYTES[dom] / (mean_k[dom] * 1e-3) / 1e9
-    traffic = _load_traffic({"r2c": "k_r2c_even", "conv": "k_conv", "c2r": "k_c2r_even"}[dom])
+    traffic = _load_traffic({"r2c": "k_r2c_even", "conv": "k_conv_pf", "c2r": "k_c2r_even"}[dom])
 
     # End to end through the public API.  Every step uploads its input from
     # pinned host memory into an RFFTBuffer (its own packed layout, rows of

@@ -136,16 +136,21 @@ __device__ __forceinline__ void run_unit(const BatchArgs& a, const WorkUnit* __r
   Cx<float>* dst = (kind == UK_COLS ? a.ws : a.data) + wu.dst + pl.m * wu.dst_slot;
   const int dst_pt = int(wu.dst_pt);
   const bool twiddle = cols;
-  const Cx<float> sc = mk<float>(wu.scale, 0.f);
+  const float sc = wu.scale;
   const Cx<float>* twl = wu.twl;
   const int twstep = twiddle ? wu.c0 + pl.m : 0;  // n2; n2 * k1 < L <= 2^24
   radix_dispatch(pp.radix[pp.npass - 1], [&](auto rc) {
     constexpr int RR = decltype(rc)::value;
     each_natural<RR, MAXE, float>(v, n / RR, T, pl.t, [&](int pos, Cx<float> val) {
       if (!valid) return;
-      // W_L^{n2 k1} with n2 = column, k1 = pos (n2 k1 < L), or the scale
-      const Cx<float> w = twiddle ? ldg(twl + twstep * pos) : sc;
-      dst[pos * dst_pt] = INV ? cmulc(val, w) : cmul(val, w);
+      if (twiddle) {
+        // W_L^{n2 k1} with n2 = column, k1 = pos (n2 k1 < L)
+        const Cx<float> w = ldg(twl + twstep * pos);
+        val = INV ? cmulc(val, w) : cmul(val, w);
+      } else {
+        val = scale(val, sc);
+      }
+      dst[pos * dst_pt] = val;
     });
   });
 }
