@@ -292,18 +292,20 @@ def test_from_cuda_array_checks():
         vd.from_cuda_array(t, var_type=vd.complex128)
 
 
+@pytest.mark.parametrize("pts", [8, 32])
 @pytest.mark.parametrize("kop_conj", [True, False])
-def test_strided_convolution_eight_points_per_thread(monkeypatch, kop_conj):
-    """The radix-8 compile-time plan (64 threads per 512-point column) of the
-    strided fused convolution matches FP64 numpy, conjugate and plain product."""
+def test_strided_convolution_points_per_thread(monkeypatch, kop_conj, pts):
+    """The alternative compile-time plans of the strided fused convolution
+    (radix 8 x 8 x 8 with 64 threads per 512-point column, radix 32 x 16 with
+    16) match FP64 numpy, conjugate and plain product."""
     import torch
 
     from vkdispatch_gb300 import _lib as L
     from vkdispatch_gb300.fft import plan as P
 
-    monkeypatch.setenv("VDX_CONV_POINTS_PER_THREAD", "8")
+    monkeypatch.setenv("VDX_CONV_POINTS_PER_THREAD", str(pts))
     P.cache_clear()
-    rng = np.random.default_rng(31 + kop_conj)
+    rng = np.random.default_rng(31 + kop_conj + pts)
     shape = (3, 512, 257)
     x = crandn(rng, shape)
     k = crandn(rng, shape)
@@ -311,7 +313,8 @@ def test_strided_convolution_eight_points_per_thread(monkeypatch, kop_conj):
     kop = L.VDX_KOP_MUL_CONJ if kop_conj else L.VDX_KOP_MUL
     p = P.get_plan(shape, 1, L.VDX_KIND_CONV, False, True, L.VDX_C64, L.VDX_C64, None, kop, L.VDX_C64)
     d = p.describe()
-    assert d["threads_per_transform"] == 64 and d["radices"] == "8x8x8" and d["fixed"] is True
+    assert d["threads_per_transform"] == 512 // pts and d["fixed"] is True
+    assert d["radices"] == {8: "8x8x8", 32: "32x16"}[pts]
     p.exec(xt.data_ptr(), xt.data_ptr(), kt.data_ptr(), torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     s = np.fft.fft(x.astype(np.complex128), axis=1)

@@ -1,8 +1,8 @@
 // complex64 FFT kernels specialised for n = 512 (and the strided convolution
-// with 8 points per thread).
+// with 8 or 32 points per thread).
 #include "fft_launch.cuh"
 
 namespace vdx {
 template cudaError_t launch_fixed_c64<512>(const FftArgs&, const Launch&, int, bool, int, int);
-template cudaError_t launch_fixed8_conv_c64<512>(const FftArgs&, const Launch&, int, int);
+template cudaError_t launch_fixedpts_conv_c64<512>(int, const FftArgs&, const Launch&, int, int);
 }  // namespace vdx

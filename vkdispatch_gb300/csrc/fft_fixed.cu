@@ -25,11 +25,11 @@ cudaError_t launch_fixed_c64_any(int n, const FftArgs& a, const Launch& l, int o
   }
 }
 
-bool has_fixed8_conv_c64(int n) { return n == 512; }
+bool has_fixedpts_conv_c64(int n, int pts) { return n == 512 && (pts == 8 || pts == 32); }
 
-cudaError_t launch_fixed8_conv_c64_any(int n, const FftArgs& a, const Launch& l, int kop, int variant) {
+cudaError_t launch_fixedpts_conv_c64_any(int n, int pts, const FftArgs& a, const Launch& l, int kop, int variant) {
   switch (n) {
-    case 512: return launch_fixed8_conv_c64<512>(a, l, kop, variant);
+    case 512: return launch_fixedpts_conv_c64<512>(pts, a, l, kop, variant);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -561,7 +561,10 @@ __global__ void __launch_bounds__(1024) k_conv(FftArgs a) {
 }
 
 // Strided fused convolution for CTAs of at most 256 threads, complex64 (two
-// CTAs per SM with 16 points per thread, three with 8).
+// CTAs per SM with 16 or 32 points per thread, three with 8).  Plans of up
+// to 16 points per thread hold the kernel spectrum in registers from the
+// start; with 32 the registers are full and it is loaded after the forward
+// FFT.
 // The signal loads are issued first and the kernel-spectrum loads right
 // after them, into registers, so the kernel spectrum's HBM latency overlaps
 // the forward passes instead of following them (the registers it takes need
@@ -579,10 +582,11 @@ __global__ void __launch_bounds__(256, Plan::MAXE <= 8 ? 3 : 2) k_conv_pf(FftArg
   P.assume_t(pl.t);
   const int n = P.n();
   const bool kvalid = pl.tile_full || pl.valid;
+  constexpr bool PF = MAXE <= 16;
   Cx<Re> v[MAXE];
   gather_input<Plan, S, Re>(P, pl, a, v, in);
-  Cx<Re> kr[MAXE];
-  P.template last<false>([&](auto rc) {
+  Cx<Re> kr[PF ? MAXE : 1];
+  if constexpr (PF) P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
     constexpr int B = MAXE / RR;
     const int nb = n / RR;
@@ -598,11 +602,20 @@ __global__ void __launch_bounds__(256, Plan::MAXE <= 8 ? 3 : 2) k_conv_pf(FftArg
   P.template last<false>([&](auto rc) {
     constexpr int RR = decltype(rc)::value;
     constexpr int B = MAXE / RR;
+    const int nb = n / RR;
 #pragma unroll
     for (int b = 0; b < B; ++b)
 #pragma unroll
-      for (int r = 0; r < RR; ++r)
-        v[b * RR + r] = KOP == 0 ? cmulc(v[b * RR + r], kr[b * RR + r]) : cmul(v[b * RR + r], kr[b * RR + r]);
+      for (int r = 0; r < RR; ++r) {
+        Cx<Re> k;
+        if constexpr (PF) {
+          k = kr[b * RR + r];
+        } else {
+          const int j = pl.t + b * P.T();
+          k = (j < nb && kvalid) ? ld_once<S, Re>(ker + (j + r * nb) * pl.ps) : mk<Re>(Re(0), Re(0));
+        }
+        v[b * RR + r] = KOP == 0 ? cmulc(v[b * RR + r], k) : cmul(v[b * RR + r], k);
+      }
   });
   P.template run<true, true>(v, pl, sm, tw);
   store_output<Plan, true, S, Re>(P, pl, a, v);
@@ -824,6 +837,15 @@ template <> struct Pow2x8<512> { using L = RList<8, 8, 8>; static constexpr int 
 
 template <int N>
 using Pow2x8Plan = FixPlan<N, Pow2x8<N>::T, typename Pow2x8<N>::L, 8>;
+
+// two-pass compile-time plans, 32 points per thread (n/32 threads per
+// transform): one shared-memory exchange per FFT instead of two
+template <int N>
+struct Pow2x32;
+template <> struct Pow2x32<512> { using L = RList<32, 16>; static constexpr int T = 16; };
+
+template <int N>
+using Pow2x32Plan = FixPlan<N, Pow2x32<N>::T, typename Pow2x32<N>::L, 32>;
 
 
 }  // namespace vdx

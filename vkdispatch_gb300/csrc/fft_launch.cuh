@@ -139,11 +139,15 @@ cudaError_t launch_fixed_c64(const FftArgs& a, const Launch& l, int op, bool str
   return launch_with_plan<Pow2Plan<N>, Cx<float>, float, false>(a, l, op, strided, kop, variant);
 }
 
-// strided complex64 convolution with the 8-points-per-thread plan
+// strided complex64 convolution with the 8- or 32-points-per-thread plan
 template <int N>
-cudaError_t launch_fixed8_conv_c64(const FftArgs& a, const Launch& l, int kop, int variant) {
-  if (kop == 0) return launch_conv_layout<Pow2x8Plan<N>, 0, true, Cx<float>, float>(a, l, variant);
-  return launch_conv_layout<Pow2x8Plan<N>, 1, true, Cx<float>, float>(a, l, variant);
+cudaError_t launch_fixedpts_conv_c64(int pts, const FftArgs& a, const Launch& l, int kop, int variant) {
+  if (pts == 8) {
+    if (kop == 0) return launch_conv_layout<Pow2x8Plan<N>, 0, true, Cx<float>, float>(a, l, variant);
+    return launch_conv_layout<Pow2x8Plan<N>, 1, true, Cx<float>, float>(a, l, variant);
+  }
+  if (kop == 0) return launch_conv_layout<Pow2x32Plan<N>, 0, true, Cx<float>, float>(a, l, variant);
+  return launch_conv_layout<Pow2x32Plan<N>, 1, true, Cx<float>, float>(a, l, variant);
 }
 
 }  // namespace vdx

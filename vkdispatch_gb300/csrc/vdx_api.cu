@@ -181,7 +181,7 @@ struct Tune {
   int order = 0;      // radix passes: 0 = largest radix first, 1 = smallest first
   int fixed = -1;     // compile-time kernels where available: -1 = yes, 0 = no
   int fourstep = -1;  // long C2C axes: -1 = from 8192 points (VDX_FOURSTEP_MIN), 0 = only above one CTA, 1 = always
-  int maxe = 16;      // points per thread: 16, or 8 (strided complex64 convolutions with a compile-time plan)
+  int maxe = 16;      // points per thread: 16, or 8 / 32 (strided complex64 convolutions with a compile-time plan)
 };
 }  // namespace vdx
 
@@ -201,7 +201,7 @@ struct vdx_plan {
   // `chunk_cols` columns x `chunk_outer` outer batches (strided axes) or
   // `chunk_outer` rows (contiguous axes); `ws` holds one chunk
   bool fourstep = false;
-  bool fixed8 = false;  // strided convolution on the 8-points-per-thread compile-time plan
+  int fixed_pts = 0;  // 8 or 32: strided convolution on that points-per-thread compile-time plan
   int N1 = 0, N0 = 0;
   long long inner = 1, outer = 1;
   long long chunk_cols = 0, chunk_outer = 0;
@@ -698,16 +698,20 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
 
   const bool even_real = real && (N % 2 == 0);
   const int n = even_real ? N / 2 : N;  // complex points per transform
-  // 8 points per thread: strided complex64 convolutions with a compile-time
-  // plan, chosen by the autotuner or by VDX_CONV_POINTS_PER_THREAD=8
-  const bool can8 = d.kind == VDX_KIND_CONV && inner > 1 && st == ST_C64 && !f64 && has_fixed8_conv_c64(N) &&
-                    tune.order == 0 && tune.fixed != 0 && std::getenv("VDX_NO_FIXED") == nullptr;
-  int pmaxe = tune.maxe == 8 ? 8 : 16;
-  if (const char* e = std::getenv("VDX_CONV_POINTS_PER_THREAD"))
-    if (std::atoi(e) == 8 && can8) pmaxe = 8;
-  if (pmaxe == 8 && !can8) {
+  // 8 or 32 points per thread: strided complex64 convolutions with a
+  // compile-time plan, chosen by the autotuner or by
+  // VDX_CONV_POINTS_PER_THREAD=8|32
+  const bool canpts = d.kind == VDX_KIND_CONV && inner > 1 && st == ST_C64 && !f64 && tune.order == 0 &&
+                      tune.fixed != 0 && std::getenv("VDX_NO_FIXED") == nullptr;
+  int pmaxe = (tune.maxe == 8 || tune.maxe == 32) ? tune.maxe : 16;
+  if (const char* e = std::getenv("VDX_CONV_POINTS_PER_THREAD")) {
+    const int v = std::atoi(e);
+    if ((v == 8 || v == 32) && canpts && has_fixedpts_conv_c64(N, v)) pmaxe = v;
+  }
+  if (pmaxe != 16 && !(canpts && has_fixedpts_conv_c64(N, pmaxe))) {
     delete p;
-    return fail(VDX_ERR_UNSUPPORTED, "8 points per thread exist for strided complex64 convolutions of 512 points");
+    return fail(VDX_ERR_UNSUPPORTED,
+                "8 or 32 points per thread exist for strided complex64 convolutions of 512 points");
   }
   const int maxe = f64 ? MaxE<double>::value : (pmaxe == 8 ? 8 : MaxE<float>::value);
   std::string why;
@@ -718,12 +722,13 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
     return fail(VDX_ERR_UNSUPPORTED, why + " (VDX_FFT_FLAG_BLUESTEIN plans such lengths)");
   }
   if (tune.order == 1) std::reverse(p->radices.begin(), p->radices.end());
+  if (pmaxe == 32) p->radices = {32, 16};  // the two-pass compile-time plan
 
   // threads per transform: enough that every pass fits in MAXE registers
   int T = 1;
   for (int r : p->radices) {
     const int nb = n / r;
-    const int per = std::max(1, maxe / r);
+    const int per = std::max(1, (pmaxe == 32 ? 32 : maxe) / r);
     T = std::max(T, (nb + per - 1) / per);
   }
   int smem_optin = 0;
@@ -862,8 +867,8 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
   p->fixed = st == ST_C64 && !f64 && has_fixed_c64(n) && p->op != OP_R2C_ODD &&
              p->op != OP_C2R_ODD && T == n / 16 && std::getenv("VDX_NO_FIXED") == nullptr && tune.order == 0 &&
              tune.fixed != 0;
-  p->fixed8 = pmaxe == 8 && T == n / 8 && p->op == OP_CONV && strided;
-  if (pmaxe == 8 && !p->fixed8) {
+  p->fixed_pts = (pmaxe != 16 && T == n / pmaxe && p->op == OP_CONV && strided) ? pmaxe : 0;
+  if (pmaxe != 16 && !p->fixed_pts) {
     delete p;
     return fail(VDX_ERR_UNSUPPORTED, "no compile-time plan of 8 points per thread for this convolution");
   }
@@ -1033,14 +1038,16 @@ int autotune_plan(const vdx_fft_desc& d0, vdx_plan** plan) {
             t.fourstep = fsv;
             cands.push_back(t);
           }
-    // strided complex64 convolutions: the 8-points-per-thread compile-time plan
+    // strided complex64 convolutions: the 8- and 32-points-per-thread
+    // compile-time plans
     if (d.kind == VDX_KIND_CONV && inner_t > 1 && d.io_type == VDX_C64 && d.compute_type == VDX_C64)
-      for (int w : widths) {
-        Tune t;
-        t.width = w;
-        t.maxe = 8;
-        cands.push_back(t);
-      }
+      for (int pts : {8, 32})
+        for (int w : widths) {
+          Tune t;
+          t.width = w;
+          t.maxe = pts;
+          cands.push_back(t);
+        }
     std::vector<std::string> seen;
     for (const Tune& t : cands) {
       vdx_plan* c = nullptr;
@@ -1158,7 +1165,7 @@ int vdx_autotune_load(const char* path) {
     t.order = v[13];
     t.fixed = v[14];
     t.fourstep = v[15];
-    t.maxe = v[16] == 8 ? 8 : 16;
+    t.maxe = (v[16] == 8 || v[16] == 32) ? v[16] : 16;
     g_tuned[k] = t;
     ++loaded;
   }
@@ -1206,7 +1213,7 @@ int vdx_fft_plan_describe(const vdx_plan* p, char* buf, size_t n) {
                 "\"transforms_per_cta\": %d, \"strided\": %s, \"fixed\": %s, \"grid\": %u, \"block\": %u, "
                 "\"smem\": %zu, \"autotuned\": %s, \"tune\": [%d, %d, %d, %d, %d], \"tune_candidates\": %d}",
                 ops[p->op], p->N, p->args.pp.n, r.c_str(), p->args.pp.T, p->args.pp.M, p->strided ? "true" : "false",
-                (p->fixed || p->fixed8) ? "true" : "false", p->launch.grid.x, p->launch.block.x, p->launch.smem,
+                (p->fixed || p->fixed_pts) ? "true" : "false", p->launch.grid.x, p->launch.block.x, p->launch.smem,
                 p->tuned ? "true" : "false", p->tune.width, p->tune.order, p->tune.fixed, p->tune.fourstep,
                 p->tune.maxe, p->tuned_candidates);
   return VDX_OK;
@@ -1291,8 +1298,8 @@ int exec_plan(const vdx_plan* p, const void* in, void* out, const void* kernel, 
   }
   Launch l = p->launch;
   l.stream = reinterpret_cast<cudaStream_t>(stream);
-  if (p->fixed8) {
-    e = launch_fixed8_conv_c64_any(p->args.pp.n, a, l, p->d.kernel_op, variant);
+  if (p->fixed_pts) {
+    e = launch_fixedpts_conv_c64_any(p->args.pp.n, p->fixed_pts, a, l, p->d.kernel_op, variant);
     if (e != cudaSuccess) return cuda_fail(e, "FFT launch");
     return VDX_OK;
   }

@@ -115,12 +115,13 @@ cudaError_t launch_fixed_c64(const FftArgs& a, const Launch& l, int op, bool str
 bool has_fixed_c64(int n);
 cudaError_t launch_fixed_c64_any(int n, const FftArgs& a, const Launch& l, int op, bool strided, int kop,
                                  int variant);
-// strided complex64 convolution, radix-8 passes with n/8 threads per
-// transform (n = 512)
+// strided complex64 convolution on the alternative compile-time plans of
+// n = 512: pts = 8 (radix-8 passes, n/8 threads per transform) or 32
+// (radix 32 x 16, n/32 threads per transform)
 template <int N>
-cudaError_t launch_fixed8_conv_c64(const FftArgs& a, const Launch& l, int kop, int variant);
-bool has_fixed8_conv_c64(int n);
-cudaError_t launch_fixed8_conv_c64_any(int n, const FftArgs& a, const Launch& l, int kop, int variant);
+cudaError_t launch_fixedpts_conv_c64(int pts, const FftArgs& a, const Launch& l, int kop, int variant);
+bool has_fixedpts_conv_c64(int n, int pts);
+cudaError_t launch_fixedpts_conv_c64_any(int n, int pts, const FftArgs& a, const Launch& l, int kop, int variant);
 
 // Opt a kernel into more than 48 KB of dynamic shared memory once.
 template <class K>
