@@ -303,7 +303,7 @@ def test_strided_convolution_points_per_thread(monkeypatch, kop_conj, pts):
     from vkdispatch_gb300 import _lib as L
     from vkdispatch_gb300.fft import plan as P
 
-    monkeypatch.setenv("VDX_CONV_POINTS_PER_THREAD", str(pts))
+    monkeypatch.setenv("VDX_POINTS_PER_THREAD", str(pts))
     P.cache_clear()
     rng = np.random.default_rng(31 + kop_conj + pts)
     shape = (3, 512, 257)
@@ -320,4 +320,33 @@ def test_strided_convolution_points_per_thread(monkeypatch, kop_conj, pts):
     s = np.fft.fft(x.astype(np.complex128), axis=1)
     ref = np.fft.ifft(s * (np.conj(k) if kop_conj else k), axis=1)
     assert rel_l2(xt.cpu().numpy(), ref) <= 2 * tol_fp32(512)
+    P.cache_clear()
+
+
+@pytest.mark.parametrize("shape,axis", [((96, 1024), 1), ((1024, 40), 0), ((3, 1024, 5), 1)])
+def test_c2c_1024_two_pass_plan(monkeypatch, shape, axis):
+    """The radix 32 x 32 compile-time plan (one warp per 1024-point
+    transform) matches FP64 numpy forward and inverse, contiguous and strided."""
+    import torch
+
+    from vkdispatch_gb300 import _lib as L
+    from vkdispatch_gb300.fft import plan as P
+
+    monkeypatch.setenv("VDX_POINTS_PER_THREAD", "32")
+    P.cache_clear()
+    rng = np.random.default_rng(sum(shape) + axis)
+    x = crandn(rng, shape)
+    t = torch.from_numpy(x).cuda()
+    s = torch.cuda.current_stream().cuda_stream
+    fwd = P.get_plan(shape, axis, L.VDX_KIND_C2C, False, False, L.VDX_C64, L.VDX_C64)
+    d = fwd.describe()
+    assert d["threads_per_transform"] == 32 and d["radices"] == "32x32" and d["fixed"] is True
+    fwd.exec(t.data_ptr(), t.data_ptr(), None, s)
+    torch.cuda.synchronize()
+    ref = np.fft.fft(x.astype(np.complex128), axis=axis)
+    assert rel_l2(t.cpu().numpy(), ref) <= tol_fp32(1024)
+    inv = P.get_plan(shape, axis, L.VDX_KIND_C2C, True, True, L.VDX_C64, L.VDX_C64)
+    inv.exec(t.data_ptr(), t.data_ptr(), None, s)
+    torch.cuda.synchronize()
+    assert rel_l2(t.cpu().numpy(), x) <= 2 * tol_fp32(1024)
     P.cache_clear()

@@ -25,13 +25,20 @@ cudaError_t launch_fixed_c64_any(int n, const FftArgs& a, const Launch& l, int o
   }
 }
 
-bool has_fixedpts_conv_c64(int n, int pts) { return n == 512 && (pts == 8 || pts == 32); }
+bool has_fixedpts_c64(int n, int pts, bool conv, bool strided) {
+  if (conv) return strided && n == 512 && (pts == 8 || pts == 32);
+  return n == 1024 && pts == 32;
+}
 
-cudaError_t launch_fixedpts_conv_c64_any(int n, int pts, const FftArgs& a, const Launch& l, int kop, int variant) {
-  switch (n) {
-    case 512: return launch_fixedpts_conv_c64<512>(pts, a, l, kop, variant);
-    default: return cudaErrorInvalidValue;
+cudaError_t launch_fixedpts_c64_any(int n, int pts, const FftArgs& a, const Launch& l, int op, bool strided, int kop,
+                                    int variant) {
+  if (op == OP_CONV) {
+    if (n == 512 && strided) return launch_fixedpts_conv_c64<512>(pts, a, l, kop, variant);
+    return cudaErrorInvalidValue;
   }
+  if ((op == OP_C2C_FWD || op == OP_C2C_INV) && n == 1024 && pts == 32)
+    return launch_fixedpts_c2c_c64<1024>(a, l, op, strided, variant);
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace vdx

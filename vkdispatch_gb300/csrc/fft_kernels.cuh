@@ -433,8 +433,9 @@ __device__ __forceinline__ void store_output(const Plan& P, const Place<STRIDED>
 // IW: multiply each input point by in_weight[element] * in_weight_scale as it
 // is loaded (the 2 w y of a weighted |y|^2 loss's gradient).
 // LOSS: write one partial of sum(loss_weight[element] * |output|^2) per CTA.
+// Plans of 32 points per thread run CTAs of at most 256 threads, two per SM.
 template <class Plan, bool INV, bool STRIDED, class S, class Re, int IW = 0, int LOSS = 0>
-__global__ void __launch_bounds__(1024) k_c2c(FftArgs a) {
+__global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 32 ? 2 : 1) k_c2c(FftArgs a) {
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
   const Place<STRIDED> pl(a, P.T());
@@ -843,6 +844,7 @@ using Pow2x8Plan = FixPlan<N, Pow2x8<N>::T, typename Pow2x8<N>::L, 8>;
 template <int N>
 struct Pow2x32;
 template <> struct Pow2x32<512> { using L = RList<32, 16>; static constexpr int T = 16; };
+template <> struct Pow2x32<1024> { using L = RList<32, 32>; static constexpr int T = 32; };
 
 template <int N>
 using Pow2x32Plan = FixPlan<N, Pow2x32<N>::T, typename Pow2x32<N>::L, 32>;

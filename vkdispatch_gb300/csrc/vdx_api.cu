@@ -698,20 +698,23 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
 
   const bool even_real = real && (N % 2 == 0);
   const int n = even_real ? N / 2 : N;  // complex points per transform
-  // 8 or 32 points per thread: strided complex64 convolutions with a
-  // compile-time plan, chosen by the autotuner or by
-  // VDX_CONV_POINTS_PER_THREAD=8|32
-  const bool canpts = d.kind == VDX_KIND_CONV && inner > 1 && st == ST_C64 && !f64 && tune.order == 0 &&
-                      tune.fixed != 0 && std::getenv("VDX_NO_FIXED") == nullptr;
+  // 8 or 32 points per thread: complex64 compile-time plans for strided
+  // convolutions of 512 points (8 or 32) and C2C transforms of 1024 points
+  // (32), chosen by the autotuner or by VDX_POINTS_PER_THREAD=8|32
+  const bool canpts = (d.kind == VDX_KIND_CONV || d.kind == VDX_KIND_C2C) && st == ST_C64 && !f64 &&
+                      lo == 0 && hi == N && tune.order == 0 && tune.fixed != 0 &&
+                      std::getenv("VDX_NO_FIXED") == nullptr;
+  const bool is_conv = d.kind == VDX_KIND_CONV;
   int pmaxe = (tune.maxe == 8 || tune.maxe == 32) ? tune.maxe : 16;
-  if (const char* e = std::getenv("VDX_CONV_POINTS_PER_THREAD")) {
+  if (const char* e = std::getenv("VDX_POINTS_PER_THREAD")) {
     const int v = std::atoi(e);
-    if ((v == 8 || v == 32) && canpts && has_fixedpts_conv_c64(N, v)) pmaxe = v;
+    if ((v == 8 || v == 32) && canpts && has_fixedpts_c64(N, v, is_conv, inner > 1)) pmaxe = v;
   }
-  if (pmaxe != 16 && !(canpts && has_fixedpts_conv_c64(N, pmaxe))) {
+  if (pmaxe != 16 && !(canpts && has_fixedpts_c64(N, pmaxe, is_conv, inner > 1))) {
     delete p;
     return fail(VDX_ERR_UNSUPPORTED,
-                "8 or 32 points per thread exist for strided complex64 convolutions of 512 points");
+                "8 or 32 points per thread exist for strided complex64 convolutions of 512 points and 32 for "
+                "complex64 C2C transforms of 1024 points");
   }
   const int maxe = f64 ? MaxE<double>::value : (pmaxe == 8 ? 8 : MaxE<float>::value);
   std::string why;
@@ -722,7 +725,7 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
     return fail(VDX_ERR_UNSUPPORTED, why + " (VDX_FFT_FLAG_BLUESTEIN plans such lengths)");
   }
   if (tune.order == 1) std::reverse(p->radices.begin(), p->radices.end());
-  if (pmaxe == 32) p->radices = {32, 16};  // the two-pass compile-time plan
+  if (pmaxe == 32) p->radices = {32, n / 32};  // the two-pass compile-time plan
 
   // threads per transform: enough that every pass fits in MAXE registers
   int T = 1;
@@ -785,7 +788,7 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
     if (const char* e = std::getenv("VDX_STRIDED_COLUMNS")) mcols = std::max(1, std::min(32, std::atoi(e)));
     if (tune.width > 0) mcols = std::min(32, tune.width);
     M = (int)std::min<long long>(mcols, inner);
-    M = std::max(1, std::min(M, 1024 / T));
+    M = std::max(1, std::min(M, (pmaxe == 32 ? 256 : 1024) / T));  // 32-point plans: CTAs of <= 256 threads
     while (M > 1 && need_smem && size_t(n) * M * cbytes > size_t(smem_optin)) M /= 2;
     smem = need_smem ? size_t(n) * M * cbytes : 0;
   } else {
@@ -795,7 +798,7 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
     if (tune.width > 0) cta_threads = std::max(32, std::min(1024, tune.width));
     M = std::max(1, cta_threads / T);
     M = (int)std::min<long long>(M, ntrans);
-    M = std::max(1, std::min(M, 1024 / T));
+    M = std::max(1, std::min(M, (pmaxe == 32 ? 256 : 1024) / T));  // 32-point plans: CTAs of <= 256 threads
     while (M > 1 && need_smem && size_t(npad) * M * cbytes > size_t(smem_optin) / 2) M /= 2;
     smem = need_smem ? size_t(npad) * M * cbytes : 0;
   }
@@ -867,7 +870,10 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
   p->fixed = st == ST_C64 && !f64 && has_fixed_c64(n) && p->op != OP_R2C_ODD &&
              p->op != OP_C2R_ODD && T == n / 16 && std::getenv("VDX_NO_FIXED") == nullptr && tune.order == 0 &&
              tune.fixed != 0;
-  p->fixed_pts = (pmaxe != 16 && T == n / pmaxe && p->op == OP_CONV && strided) ? pmaxe : 0;
+  p->fixed_pts = (pmaxe != 16 && T == n / pmaxe &&
+                  ((p->op == OP_CONV && strided) || p->op == OP_C2C_FWD || p->op == OP_C2C_INV))
+                     ? pmaxe
+                     : 0;
   if (pmaxe != 16 && !p->fixed_pts) {
     delete p;
     return fail(VDX_ERR_UNSUPPORTED, "no compile-time plan of 8 points per thread for this convolution");
@@ -1038,9 +1044,9 @@ int autotune_plan(const vdx_fft_desc& d0, vdx_plan** plan) {
             t.fourstep = fsv;
             cands.push_back(t);
           }
-    // strided complex64 convolutions: the 8- and 32-points-per-thread
-    // compile-time plans
-    if (d.kind == VDX_KIND_CONV && inner_t > 1 && d.io_type == VDX_C64 && d.compute_type == VDX_C64)
+    // the 8- and 32-points-per-thread compile-time plans (create_plan
+    // refuses the combinations that have none)
+    if ((d.kind == VDX_KIND_CONV || d.kind == VDX_KIND_C2C) && d.io_type == VDX_C64 && d.compute_type == VDX_C64)
       for (int pts : {8, 32})
         for (int w : widths) {
           Tune t;
@@ -1299,7 +1305,7 @@ int exec_plan(const vdx_plan* p, const void* in, void* out, const void* kernel, 
   Launch l = p->launch;
   l.stream = reinterpret_cast<cudaStream_t>(stream);
   if (p->fixed_pts) {
-    e = launch_fixedpts_conv_c64_any(p->args.pp.n, p->fixed_pts, a, l, p->d.kernel_op, variant);
+    e = launch_fixedpts_c64_any(p->args.pp.n, p->fixed_pts, a, l, p->op, p->strided, p->d.kernel_op, variant);
     if (e != cudaSuccess) return cuda_fail(e, "FFT launch");
     return VDX_OK;
   }

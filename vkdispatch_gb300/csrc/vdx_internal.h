@@ -115,13 +115,17 @@ cudaError_t launch_fixed_c64(const FftArgs& a, const Launch& l, int op, bool str
 bool has_fixed_c64(int n);
 cudaError_t launch_fixed_c64_any(int n, const FftArgs& a, const Launch& l, int op, bool strided, int kop,
                                  int variant);
-// strided complex64 convolution on the alternative compile-time plans of
-// n = 512: pts = 8 (radix-8 passes, n/8 threads per transform) or 32
-// (radix 32 x 16, n/32 threads per transform)
+// complex64 kernels on the alternative compile-time plans: strided
+// convolutions of n = 512 with pts = 8 (radix-8 passes, n/8 threads per
+// transform) or 32 (radix 32 x 16, n/32 threads), and C2C transforms of
+// n = 1024 with pts = 32 (radix 32 x 32, one warp per transform)
 template <int N>
 cudaError_t launch_fixedpts_conv_c64(int pts, const FftArgs& a, const Launch& l, int kop, int variant);
-bool has_fixedpts_conv_c64(int n, int pts);
-cudaError_t launch_fixedpts_conv_c64_any(int n, int pts, const FftArgs& a, const Launch& l, int kop, int variant);
+template <int N>
+cudaError_t launch_fixedpts_c2c_c64(const FftArgs& a, const Launch& l, int op, bool strided, int variant);
+bool has_fixedpts_c64(int n, int pts, bool conv, bool strided);
+cudaError_t launch_fixedpts_c64_any(int n, int pts, const FftArgs& a, const Launch& l, int op, bool strided, int kop,
+                                    int variant);
 
 // Opt a kernel into more than 48 KB of dynamic shared memory once.
 template <class K>
