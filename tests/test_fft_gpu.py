@@ -350,3 +350,39 @@ def test_c2c_1024_two_pass_plan(monkeypatch, shape, axis):
     torch.cuda.synchronize()
     assert rel_l2(t.cpu().numpy(), x) <= 2 * tol_fp32(1024)
     P.cache_clear()
+
+
+@pytest.mark.parametrize("N", [1024, 2048])
+def test_real_transforms_two_pass_plan(monkeypatch, N):
+    """R2C / C2R of 1024 and 2048 real samples (512 / 1024 complex points) on
+    the two-pass radix-32 compile-time plans match FP64 numpy."""
+    monkeypatch.setenv("VDX_POINTS_PER_THREAD", "32")
+    from vkdispatch_gb300.fft import plan as P
+
+    P.cache_clear()
+    rng = np.random.default_rng(N)
+    r = rng.standard_normal((24, N)).astype(np.float32)
+    rb = vd.asrfftbuffer(r)
+    vd.fft.rfft(rb)
+    spec = np.fft.rfft(r.astype(np.float64), axis=-1)
+    assert rel_l2(rb.read_fourier(0), spec) <= tol_fp32(N)
+    vd.fft.irfft(rb)
+    assert rel_l2(rb.read_real(0), r) <= 2 * tol_fp32(N)
+    P.cache_clear()
+
+
+@pytest.mark.parametrize("n", [512, 1024])
+def test_contiguous_convolution_two_pass_plan(monkeypatch, n):
+    """The fused convolution along the contiguous axis on the two-pass plans."""
+    monkeypatch.setenv("VDX_POINTS_PER_THREAD", "32")
+    from vkdispatch_gb300.fft import plan as P
+
+    P.cache_clear()
+    rng = np.random.default_rng(n + 5)
+    x = crandn(rng, (20, n))
+    k = crandn(rng, (20, n))
+    b = vd.asbuffer(x)
+    vd.fft.convolve(b, vd.asbuffer(k))
+    ref = np.fft.ifft(np.fft.fft(x.astype(np.complex128), axis=1) * np.conj(k), axis=1)
+    assert rel_l2(b.read(0), ref) <= 2 * tol_fp32(n)
+    P.cache_clear()

@@ -26,19 +26,22 @@ cudaError_t launch_fixed_c64_any(int n, const FftArgs& a, const Launch& l, int o
 }
 
 bool has_fixedpts_c64(int n, int pts, bool conv, bool strided) {
-  if (conv) return strided && n == 512 && (pts == 8 || pts == 32);
-  return n == 1024 && pts == 32;
+  if (pts == 8) return conv && strided && n == 512;
+  return pts == 32 && (n == 512 || n == 1024);
 }
 
 cudaError_t launch_fixedpts_c64_any(int n, int pts, const FftArgs& a, const Launch& l, int op, bool strided, int kop,
                                     int variant) {
-  if (op == OP_CONV) {
-    if (n == 512 && strided) return launch_fixedpts_conv_c64<512>(pts, a, l, kop, variant);
+  if (pts == 8) {
+    if (op == OP_CONV && strided && n == 512) return launch_fixedpts_conv_c64<512>(8, a, l, kop, variant);
     return cudaErrorInvalidValue;
   }
-  if ((op == OP_C2C_FWD || op == OP_C2C_INV) && n == 1024 && pts == 32)
-    return launch_fixedpts_c2c_c64<1024>(a, l, op, strided, variant);
-  return cudaErrorInvalidValue;
+  if (pts != 32) return cudaErrorInvalidValue;
+  switch (n) {
+    case 512: return launch_fixed32_c64<512>(a, l, op, strided, kop, variant);
+    case 1024: return launch_fixed32_c64<1024>(a, l, op, strided, kop, variant);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace vdx

@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 3
 // pass).  SPEC 2: write spec_aux * conj(S) * spec_scale to spec_out instead
 // (the kernel-spectrum gradient X conj(G) / N of an FFT convolution).
 template <class Plan, bool STRIDED, class S, class K, class Re, int KOP, int SPEC = 0>
-__global__ void __launch_bounds__(1024) k_conv(FftArgs a) {
+__global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 32 ? 2 : 1) k_conv(FftArgs a) {
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
   const Place<STRIDED> pl(a, P.T());
@@ -629,7 +629,7 @@ __global__ void __launch_bounds__(256, Plan::MAXE <= 8 ? 3 : 2) k_conv_pf(FftArg
 // X[k] = (Z[k] + conj Z[n-k])/2 - i W_2n^k (Z[k] - conj Z[n-k])/2, k = 0..n
 // ---------------------------------------------------------------------------
 template <class Plan, class S, class Re>
-__global__ void __launch_bounds__(1024) k_r2c_even(FftArgs a) {
+__global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 32 ? 2 : 1) k_r2c_even(FftArgs a) {
   using SR = typename RealOf<S>::type;
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
@@ -696,7 +696,7 @@ __global__ void __launch_bounds__(1024) k_r2c_even(FftArgs a) {
 // inverse does not depend on them) -> z = IFFT_n(Z) -> x[2m] + i x[2m+1] = z[m]
 // ---------------------------------------------------------------------------
 template <class Plan, class S, class Re>
-__global__ void __launch_bounds__(1024) k_c2r_even(FftArgs a) {
+__global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 32 ? 2 : 1) k_c2r_even(FftArgs a) {
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
   const Place<false> pl(a, P.T());

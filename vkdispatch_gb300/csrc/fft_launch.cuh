@@ -150,11 +150,11 @@ cudaError_t launch_fixedpts_conv_c64(int pts, const FftArgs& a, const Launch& l,
   return launch_conv_layout<Pow2x32Plan<N>, 1, true, Cx<float>, float>(a, l, variant);
 }
 
-// complex64 C2C (either layout, with its fused variants) on the
-// 32-points-per-thread plan
+// every complex64 operation (C2C, convolution, even-length real transforms;
+// either layout) on the 32-points-per-thread plan
 template <int N>
-cudaError_t launch_fixedpts_c2c_c64(const FftArgs& a, const Launch& l, int op, bool strided, int variant) {
-  return launch_c2c_any<Pow2x32Plan<N>, Cx<float>, float>(a, l, op, strided, variant);
+cudaError_t launch_fixed32_c64(const FftArgs& a, const Launch& l, int op, bool strided, int kop, int variant) {
+  return launch_with_plan<Pow2x32Plan<N>, Cx<float>, float, false>(a, l, op, strided, kop, variant);
 }
 
 }  // namespace vdx

@@ -698,23 +698,23 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
 
   const bool even_real = real && (N % 2 == 0);
   const int n = even_real ? N / 2 : N;  // complex points per transform
-  // 8 or 32 points per thread: complex64 compile-time plans for strided
-  // convolutions of 512 points (8 or 32) and C2C transforms of 1024 points
-  // (32), chosen by the autotuner or by VDX_POINTS_PER_THREAD=8|32
-  const bool canpts = (d.kind == VDX_KIND_CONV || d.kind == VDX_KIND_C2C) && st == ST_C64 && !f64 &&
-                      lo == 0 && hi == N && tune.order == 0 && tune.fixed != 0 &&
+  // 8 or 32 points per thread: complex64 compile-time plans of two radix-32
+  // passes for 512 and 1024 complex points (any operation) and of radix-8
+  // passes for strided 512-point convolutions, chosen by the autotuner or
+  // by VDX_POINTS_PER_THREAD=8|32
+  const bool canpts = st == ST_C64 && !f64 && (!real || even_real) && tune.order == 0 && tune.fixed != 0 &&
                       std::getenv("VDX_NO_FIXED") == nullptr;
   const bool is_conv = d.kind == VDX_KIND_CONV;
   int pmaxe = (tune.maxe == 8 || tune.maxe == 32) ? tune.maxe : 16;
   if (const char* e = std::getenv("VDX_POINTS_PER_THREAD")) {
     const int v = std::atoi(e);
-    if ((v == 8 || v == 32) && canpts && has_fixedpts_c64(N, v, is_conv, inner > 1)) pmaxe = v;
+    if ((v == 8 || v == 32) && canpts && has_fixedpts_c64(n, v, is_conv, inner > 1)) pmaxe = v;
   }
-  if (pmaxe != 16 && !(canpts && has_fixedpts_c64(N, pmaxe, is_conv, inner > 1))) {
+  if (pmaxe != 16 && !(canpts && has_fixedpts_c64(n, pmaxe, is_conv, inner > 1))) {
     delete p;
     return fail(VDX_ERR_UNSUPPORTED,
-                "8 or 32 points per thread exist for strided complex64 convolutions of 512 points and 32 for "
-                "complex64 C2C transforms of 1024 points");
+                "32 points per thread exist for complex64 transforms of 512 or 1024 complex points, 8 for strided "
+                "complex64 convolutions of 512 points");
   }
   const int maxe = f64 ? MaxE<double>::value : (pmaxe == 8 ? 8 : MaxE<float>::value);
   std::string why;
@@ -870,8 +870,8 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
   p->fixed = st == ST_C64 && !f64 && has_fixed_c64(n) && p->op != OP_R2C_ODD &&
              p->op != OP_C2R_ODD && T == n / 16 && std::getenv("VDX_NO_FIXED") == nullptr && tune.order == 0 &&
              tune.fixed != 0;
-  p->fixed_pts = (pmaxe != 16 && T == n / pmaxe &&
-                  ((p->op == OP_CONV && strided) || p->op == OP_C2C_FWD || p->op == OP_C2C_INV))
+  p->fixed_pts = (pmaxe != 16 && T == n / pmaxe && p->op != OP_R2C_ODD && p->op != OP_C2R_ODD &&
+                  (pmaxe == 32 || (p->op == OP_CONV && strided)))
                      ? pmaxe
                      : 0;
   if (pmaxe != 16 && !p->fixed_pts) {
@@ -1046,7 +1046,7 @@ int autotune_plan(const vdx_fft_desc& d0, vdx_plan** plan) {
           }
     // the 8- and 32-points-per-thread compile-time plans (create_plan
     // refuses the combinations that have none)
-    if ((d.kind == VDX_KIND_CONV || d.kind == VDX_KIND_C2C) && d.io_type == VDX_C64 && d.compute_type == VDX_C64)
+    if (d.io_type == VDX_C64 && d.compute_type == VDX_C64)
       for (int pts : {8, 32})
         for (int w : widths) {
           Tune t;

@@ -115,14 +115,14 @@ cudaError_t launch_fixed_c64(const FftArgs& a, const Launch& l, int op, bool str
 bool has_fixed_c64(int n);
 cudaError_t launch_fixed_c64_any(int n, const FftArgs& a, const Launch& l, int op, bool strided, int kop,
                                  int variant);
-// complex64 kernels on the alternative compile-time plans: strided
-// convolutions of n = 512 with pts = 8 (radix-8 passes, n/8 threads per
-// transform) or 32 (radix 32 x 16, n/32 threads), and C2C transforms of
-// n = 1024 with pts = 32 (radix 32 x 32, one warp per transform)
+// complex64 kernels on the alternative compile-time plans: pts = 32 (two
+// passes: radix 32 x 16 for n = 512, 32 x 32 for n = 1024; n/32 threads per
+// transform) for every operation, and pts = 8 (radix-8 passes, n/8 threads)
+// for strided convolutions of n = 512
 template <int N>
 cudaError_t launch_fixedpts_conv_c64(int pts, const FftArgs& a, const Launch& l, int kop, int variant);
 template <int N>
-cudaError_t launch_fixedpts_c2c_c64(const FftArgs& a, const Launch& l, int op, bool strided, int variant);
+cudaError_t launch_fixed32_c64(const FftArgs& a, const Launch& l, int op, bool strided, int kop, int variant);
 bool has_fixedpts_c64(int n, int pts, bool conv, bool strided);
 cudaError_t launch_fixedpts_c64_any(int n, int pts, const FftArgs& a, const Launch& l, int op, bool strided, int kop,
                                     int variant);
