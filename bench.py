@@ -312,13 +312,13 @@ def _run_ours(args):
     e2e_err = float(np.linalg.norm((last - ref).ravel()) / np.linalg.norm(ref.ravel()))
     e2e_bytes = h_in.numel() * 4
 
-    extra = cfg1_numbers(vd, torch, flush, args) if rank == 0 and not args.quick else {}
+    extra = c2c1024_numbers(vd, torch, flush, args) if rank == 0 and not args.quick else {}
     if rank == 0 and not args.quick:
-        extra["cfg2_rfft2_irfft2_roundtrip"] = roundtrip_numbers(vd, torch, flush, images)
+        extra["rfft2_irfft2_roundtrip_64x512x512"] = roundtrip_numbers(vd, torch, flush, images)
     if rank == 0 and not args.quick:
-        extra["cfg3_diff_conv3d_256"] = cfg3_numbers(torch, flush)
-        extra["cfg4_batched_uneven"] = cfg4_numbers(torch)
-        extra["cfg5_mixed_precision_2d_16384"] = cfg5_numbers(torch)
+        extra["diff_conv3d_256"] = diff_conv3d_numbers(torch, flush)
+        extra["batched_uneven_4096_lengths_2p28"] = batched_uneven_numbers(torch)
+        extra["mixed_precision_fft2_16384"] = mixed_precision_numbers(torch)
     cpu = cpu_baseline(images, kernel) if (rank == 0 and not args.quick) else None
 
     if rank == 0:
@@ -375,7 +375,7 @@ def _run_ours(args):
         dist.destroy_process_group()
 
 
-def cfg1_numbers(vd, torch, flush, args):
+def c2c1024_numbers(vd, torch, flush, args):
     """Plain batched C2C (N=1024): the 2 MiB case (fwd + inv + magnitude sum)
     and the HBM-scale variant (batch 262,144 = 2 GiB, L2 flushed)."""
     out = {}
@@ -405,7 +405,7 @@ def cfg1_numbers(vd, torch, flush, args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / n
     s = float(r.read(0)[0])
-    out["cfg1_256x1024_fwd_inv_magsum"] = {"ms_per_step": round(ms, 5),
+    out["c2c_256x1024_fwd_inv_magsum"] = {"ms_per_step": round(ms, 5),
                                            "GBps": round(10485760 / (ms * 1e-3) / 1e9, 1),
                                            "magnitude_sum": s, "launches_per_step": 4}
     # the same step captured once in a CUDA graph (vd.cuda_graph_capture) and
@@ -428,11 +428,11 @@ def cfg1_numbers(vd, torch, flush, args):
         e1.record()
         torch.cuda.synchronize()
         gms = e0.elapsed_time(e1) / n
-        out["cfg1_256x1024_fwd_inv_magsum"].update({
+        out["c2c_256x1024_fwd_inv_magsum"].update({
             "graph_ms_per_step": round(gms, 5), "graph_GBps": round(10485760 / (gms * 1e-3) / 1e9, 1),
             "graph_magnitude_sum": float(rg.read(0)[0])})
     except Exception as exc:  # report, do not fail the benchmark
-        out["cfg1_256x1024_fwd_inv_magsum"]["graph_error"] = str(exc)[:200]
+        out["c2c_256x1024_fwd_inv_magsum"]["graph_error"] = str(exc)[:200]
 
     big = torch.empty((262144, 1024), dtype=torch.complex64, device="cuda")
     big.normal_()
@@ -453,13 +453,13 @@ def cfg1_numbers(vd, torch, flush, args):
         t = statistics.median(ts)
         gbps = 2 * big.numel() * 8 / (t * 1e-3) / 1e9
         res[name] = {"ms": round(t, 4), "GBps": round(gbps, 1), "frac_of_measured_hbm": round(gbps / peak, 4)}
-    out["cfg1_hbm_1024x262144"] = res
+    out["c2c_hbm_1024x262144"] = res
     del big
     return out
 
 
 def roundtrip_numbers(vd, torch, flush, images, steps=20):
-    """The rfft2 -> irfft2 round trip of the Cfg2 images (64 x 512x512 f32):
+    """The rfft2 -> irfft2 round trip of the benchmark images (64 x 512x512 f32):
     rfft of the rows, FFT of the 257 spectrum columns, inverse, irfft of the
     rows.  Algorithmic bytes: each of the 4 passes reads and writes its array
     once (real rows 64 MiB, half spectrum 67,371,008 B)."""
@@ -489,7 +489,7 @@ def roundtrip_numbers(vd, torch, flush, images, steps=20):
             "rfft2_rel_l2_vs_fp64": spec_err, "roundtrip_rel_l2": rt_err}
 
 
-def cfg3_numbers(torch, flush, steps=10):
+def diff_conv3d_numbers(torch, flush, steps=10):
     """Differentiable 3-D FFT convolution, 256^3 complex64: loss = sum(w |y|^2),
     y = IFFT3(FFT3(x) conj(K)); forward + backward (grads for x and K) with
     the fused kernels vs the plain per-axis kernels + separate element-wise
@@ -558,7 +558,7 @@ def cfg3_numbers(torch, flush, steps=10):
     return out
 
 
-def cfg4_workload(total=2 ** 28, nitems=4096, seed=3):
+def uneven_workload(total=2 ** 28, nitems=4096, seed=3):
     """4096 lengths drawn log-uniformly from the 7-smooth integers in
     [16, 65536] (nearest in log distance), batch counts b_i = max(1,
     round(2^28 / (4096 L_i))), the last count trimmed so the points fit 2^28."""
@@ -574,7 +574,7 @@ def cfg4_workload(total=2 ** 28, nitems=4096, seed=3):
     return lengths, counts, len(smooth)
 
 
-def cfg4_numbers(torch, reps=10):
+def batched_uneven_numbers(torch, reps=10):
     """Batched uneven lengths: one persistent launch (replayed as a CUDA
     graph) vs one plain launch per length, issued directly and as a
     captured graph; algorithmic bytes = read + write of every point once per
@@ -584,7 +584,7 @@ def cfg4_numbers(torch, reps=10):
     from vkdispatch_gb300.batch import BatchPlan, pack_items
     from vkdispatch_gb300.fft import plan as P
 
-    lengths, counts, nsmooth = cfg4_workload()
+    lengths, counts, nsmooth = uneven_workload()
     items, points = pack_items(zip(lengths, counts))
     g = torch.Generator(device="cuda").manual_seed(3)
     data = torch.randn(points, dtype=torch.complex64, device="cuda", generator=g)
@@ -681,10 +681,10 @@ def cfg4_numbers(torch, reps=10):
     }
 
 
-CFG5_N = 16384
+FFT2_N = 16384
 
 
-def _cfg5_plan(axis, io, flags, **env):
+def _fft2_16384_plan(axis, io, flags, **env):
     """An uncached 16384 x 16384 C2C plan, orthonormal scaling (1/sqrt(N) per
     axis keeps fp16-stored spectra in range), created under `env`."""
     from vkdispatch_gb300 import _lib as L
@@ -692,7 +692,7 @@ def _cfg5_plan(axis, io, flags, **env):
 
     d = L.FftDesc()
     d.ndim = 2
-    d.shape[0] = d.shape[1] = CFG5_N
+    d.shape[0] = d.shape[1] = FFT2_N
     d.axis = axis
     d.kind = L.VDX_KIND_C2C
     d.normalize = 2
@@ -713,7 +713,7 @@ def _cfg5_plan(axis, io, flags, **env):
                 os.environ[k] = v
 
 
-def cfg5_numbers(torch, reps=10):
+def mixed_precision_numbers(torch, reps=10):
     """Mixed-precision 2-D C2C FFT of 16384 x 16384 points, re and im N(0,1)
     (torch generator, seed 4), orthonormal scaling.  Storage complex64
     (8 B/point), bf16 pairs and fp16 pairs (4 B/point); short transforms on
@@ -727,7 +727,7 @@ def cfg5_numbers(torch, reps=10):
 
     from vkdispatch_gb300 import _lib as L
 
-    N = CFG5_N
+    N = FFT2_N
     g = torch.Generator(device="cuda").manual_seed(4)
     x = torch.view_as_complex(torch.randn((N, N, 2), dtype=torch.float32, device="cuda", generator=g))
     peak, _ = _load_peaks()
@@ -755,7 +755,7 @@ def cfg5_numbers(torch, reps=10):
             data = torch.view_as_real(x).to(dt).contiguous()
             stored = torch.view_as_complex(data.float())  # a copy, taken before any transform
         x0 = data.clone()
-        plans = [_cfg5_plan(ax, io, flags, **env) for ax in (0, 1)]
+        plans = [_fft2_16384_plan(ax, io, flags, **env) for ax in (0, 1)]
         ptr = data.data_ptr()
 
         def fft2():
@@ -909,11 +909,11 @@ def _run_profile(args):
     import vkdispatch_gb300 as vd
 
     torch.cuda.set_device(0)
-    if args.profile == "cfg4small":
+    if args.profile == "batch_uneven_2p25":
         # the batched-uneven distribution at 1/8 scale (2^25 points, 512 items)
         from vkdispatch_gb300.batch import BatchPlan, pack_items
 
-        lengths, counts, _ = cfg4_workload(total=2 ** 25, nitems=512)
+        lengths, counts, _ = uneven_workload(total=2 ** 25, nitems=512)
         items, points = pack_items(zip(lengths, counts))
         data = torch.randn(points, dtype=torch.complex64, device="cuda")
         plan = BatchPlan(items)
@@ -923,14 +923,14 @@ def _run_profile(args):
         torch.cuda.synchronize()
         print("profile case done", plan.describe(), flush=True)
         return
-    if args.profile in ("cfg5small", "cfg5small_fp32"):
+    if args.profile in ("fs16384x4096_tc", "fs16384x4096_fp32"):
         # four-step passes on 16384 x 4096 bf16 pairs (256 MiB), axis 0; the
         # tensor-core short transforms or the fp32 butterflies
         from vkdispatch_gb300 import _lib as L
         from vkdispatch_gb300.fft import plan as P
 
         x = torch.randn((16384, 4096, 2), dtype=torch.float32, device="cuda").to(torch.bfloat16)
-        with vd.fft.tensor_core_stages(args.profile == "cfg5small"):
+        with vd.fft.tensor_core_stages(args.profile == "fs16384x4096_tc"):
             p = P.get_plan((16384, 4096), 0, L.VDX_KIND_C2C, False, False, L.VDX_BF16X2, L.VDX_C64)
         s = int(torch.cuda.current_stream().cuda_stream)
         for _ in range(args.steps):
