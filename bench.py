@@ -938,6 +938,28 @@ def _run_profile(args):
         torch.cuda.synchronize()
         print("profile case done", p.describe(), flush=True)
         return
+    if args.profile == "diff_conv3d_256":
+        # the fused differentiable 3-D convolution, forward + backward; the
+        # backward's launches come from autograd's device thread, outside
+        # this thread's NVTX range
+        import vkdispatch_gb300.autograd as ag
+
+        n = 256
+        g = torch.Generator(device="cuda").manual_seed(2)
+        x = torch.randn((n, n, n), dtype=torch.complex64, device="cuda", generator=g).requires_grad_(True)
+        k = (0.1 * torch.randn((n, n, n), dtype=torch.complex64, device="cuda", generator=g)).requires_grad_(True)
+        w = torch.rand((n, n, n), device="cuda", generator=g)
+        ag.conv_weighted_sqnorm(x, k, w).backward()  # plans (and their tuning) before the range
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("profile")
+        for _ in range(args.steps):
+            x.grad = None
+            k.grad = None
+            ag.conv_weighted_sqnorm(x, k, w).backward()
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.synchronize()
+        print("profile case done", flush=True)
+        return
     if args.profile == "conv2d":
         images, kernel = make_inputs()
         kb = vd.asrfftbuffer(kernel)
@@ -975,7 +997,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip the extra configs and the CPU baseline")
-    ap.add_argument("--profile", default=None, help="run a small case for ncu: conv2d or c2c<N>")
+    ap.add_argument("--profile", default=None,
+                    help="run a small case for ncu: conv2d, c2c<N>, diff_conv3d_256, batch_uneven_2p25, "
+                         "fs16384x4096_tc or fs16384x4096_fp32")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)
