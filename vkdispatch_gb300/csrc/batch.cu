@@ -104,15 +104,16 @@ __device__ __forceinline__ void run_unit(const BatchArgs& a, const WorkUnit* __r
   const bool cols = kind == UK_COLS;
   UnitPlace pl;
   const int tid = threadIdx.x;
+  // thread index split by the plan's multiply-high reciprocals (tid < 1024)
   if (cols) {
-    pl.m = tid % M;
-    pl.t = tid / M;
+    pl.t = M > 1 ? int(__umulhi(unsigned(tid), pp.mmag)) : tid;
+    pl.m = tid - pl.t * M;
     pl.ci = M;
     pl.cmo = pl.m;
     pl.cp = 0;
   } else {
-    pl.t = tid % T;
-    pl.m = tid / T;
+    pl.m = T > 1 ? int(__umulhi(unsigned(tid), pp.tmag)) : tid;
+    pl.t = tid - pl.m * T;
     pl.ci = 1;
     pl.cmo = pl.m * pp.npad;
     pl.cp = 1;
@@ -352,6 +353,7 @@ int vdx_batch_plan_create(const vdx_batch_item* items, int nitems, int inverse, 
     up.pp.T = T;
     up.pp.M = M;
     up.pp.npad = npad;
+    set_pass_tables(up.pp);
     void* tw = nullptr;
     if (get_twiddle_table(dev, n, n, false, &tw) != VDX_OK) return -4;
     up.tw = reinterpret_cast<const Cx<float>*>(tw);

@@ -32,7 +32,29 @@ struct PassPlan {
   int T;     // threads per transform
   int M;     // transforms (rows or columns) per CTA
   int npad;  // shared-memory slots per transform (contiguous layout)
+  // per-pass index constants of the runtime passes in forward order, set by
+  // set_pass_tables (0 = not set: the kernels derive them): the twiddle
+  // stride n / (ns R) and inv_magic(ns), ns = product of the earlier radices
+  int tws[kMaxPasses];
+  unsigned nsm[kMaxPasses];
+  unsigned tmag, mmag;  // inv_magic(T), inv_magic(M) where a kernel splits thread indices with them
 };
+
+// m = ceil(2^32 / d) for d >= 2 (0 for d < 2), the multiplier of mod_inv
+__host__ __device__ __forceinline__ unsigned inv_magic(int d) { return d > 1 ? 0xFFFFFFFFu / unsigned(d) + 1u : 0u; }
+
+// Fills the per-pass constants of a pass plan whose n and radix list are set.
+inline void set_pass_tables(PassPlan& pp) {
+  int ns = 1;
+  for (int q = 0; q < pp.npass; ++q) {
+    const int R = pp.radix[q];
+    pp.tws[q] = pp.n / (ns * R);
+    pp.nsm[q] = inv_magic(ns);
+    ns *= R;
+  }
+  pp.tmag = inv_magic(pp.T);
+  pp.mmag = inv_magic(pp.M);
+}
 
 struct FftArgs {
   PassPlan pp;
@@ -195,7 +217,6 @@ __device__ __forceinline__ void each_natural(Cx<Re>* v, int nb, int T, int t, F&
 __device__ __forceinline__ int mod_inv(int j, int d, unsigned m) {
   return j - int(__umulhi(unsigned(j), m)) * d;
 }
-__host__ __device__ __forceinline__ unsigned inv_magic(int d) { return d > 1 ? 0xFFFFFFFFu / unsigned(d) + 1u : 0u; }
 
 // RT: ns is a runtime value with nsm = inv_magic(ns) and tws = n / (ns R);
 // otherwise ns is a compile-time constant and j % ns folds
@@ -248,8 +269,11 @@ __device__ __forceinline__ void run_passes(Cx<Re>* v, const PassPlan& pp, bool r
     const int p = reversed ? P - 1 - q : q;
     const int R = pp.radix[p];
     const bool more = q + 1 < P;
-    const unsigned nsm = inv_magic(ns);  // one division per pass instead of one per butterfly index
-    const int tws = n / (ns * R);       // twiddle stride of the pass
+    // per-pass constants: from the plan's tables when it has them (forward
+    // order), else one division each per pass
+    const bool tab = !reversed && pp.tws[p] > 0;
+    const unsigned nsm = tab ? pp.nsm[p] : inv_magic(ns);
+    const int tws = tab ? pp.tws[p] : n / (ns * R);
     // one radix dispatch per pass covers the butterflies and the scatter
     radix_dispatch(R, [&](auto rc) {
       constexpr int RR = decltype(rc)::value;

@@ -258,6 +258,7 @@ int sub_pass_plan(int n, int M, PassPlan& pp, std::string& why) {
   pp.T = T;
   pp.M = M;
   pp.npad = n + 1 + ((n + 1) >> 4) + 1;
+  set_pass_tables(pp);
   return VDX_OK;
 }
 
@@ -300,6 +301,8 @@ int plan_fourstep(vdx_plan* p, long long inner, long long outer, int smem_optin)
   const bool strided = inner > 1;
   ppA.M = tile_m(N1, strided ? inner : N0, ppA.T);
   ppB.M = tile_m(N0, strided ? inner : N1, ppB.T);
+  ppA.mmag = inv_magic(ppA.M);
+  ppB.mmag = inv_magic(ppB.M);
   if (ppA.T * ppA.M > 512 || ppB.T * ppB.M > 512)
     return fail(VDX_ERR_UNSUPPORTED, "four-step sub-transform needs more than 512 threads");
 
@@ -817,6 +820,7 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
   a.pp.T = T;
   a.pp.M = M;
   a.pp.npad = npad;
+  set_pass_tables(a.pp);
   a.sig_lo = lo;
   a.sig_hi = hi;
   a.nreal = N;
