@@ -58,6 +58,20 @@ class Buffer:
             self._t = t
             self._keepalive = keep
 
+    @classmethod
+    def _empty(cls, shape: Tuple[int, ...], var_type: dt.dtype) -> "Buffer":
+        """A new device buffer of a shape already checked by the caller (the
+        result buffers of repeated reductions)."""
+        b = cls.__new__(cls)
+        b.shape = shape
+        b.var_type = var_type
+        b.size = math.prod(shape)
+        b.writable = True
+        b._keepalive = None
+        lane_shape = shape + ((var_type.lanes,) if var_type.lanes > 1 else ())
+        b._t = torch.empty(lane_shape, dtype=var_type.torch_dtype, device=_device())
+        return b
+
     # -- properties -----------------------------------------------------
     @property
     def ptr(self) -> int:

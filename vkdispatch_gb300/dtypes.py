@@ -27,7 +27,7 @@ class dtype:
         return hash(self.name)
 
     def __eq__(self, other):
-        return isinstance(other, dtype) and other.name == self.name
+        return self is other or (isinstance(other, dtype) and other.name == self.name)
 
 
 float16 = dtype("float16", 2, np.float16, torch.float16, 1, None)

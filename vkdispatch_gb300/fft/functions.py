@@ -24,6 +24,10 @@ from .maps import read_op, write_op  # noqa: F401
 
 _PRECISION_ORDER = (dt.complex32, dt.complex64, dt.complex128)
 
+# validated get_plan arguments of the plain in-place path of fft(), keyed by
+# the call's arguments: repeated calls skip the dtype and shape checks
+_plain_args = {}
+
 
 def _validate_complex(t, arg: str) -> None:
     if t not in _PRECISION_ORDER and t != dt.complexbf16:
@@ -223,6 +227,17 @@ def fft(
                 out_buf, out_kind, in_buf, in_kind, shape, compute, graph)
         return
     buf = buffers[0]
+    memo_key = (buf.var_type, buf.shape, buf.size, None if buffer_shape is None else tuple(buffer_shape), axis,
+                bool(inverse), bool(normalize_inverse), bool(r2c), output_type, input_type, compute_type,
+                None if input_signal_range is None else tuple(input_signal_range))
+    args = _plain_args.get(memo_key)
+    if args is not None:
+        plan = P.get_plan(*args)
+        if print_shader:
+            print(plan.describe())
+        ptr = buf.ptr
+        _record(graph, lambda s: plan.exec(ptr, ptr, None, s), (buf,))
+        return
     if buffer_shape is None:
         buffer_shape = buf.shape
     buffer_shape = tuple(int(s) for s in buffer_shape)
@@ -254,16 +269,10 @@ def fft(
         if math.prod(buffer_shape) > buf.size:
             raise ValueError(f"buffer_shape {buffer_shape} exceeds the buffer size {buf.size}")
         kind = L.VDX_KIND_C2C
-    plan = P.get_plan(
-        buffer_shape,
-        ax,
-        kind,
-        inverse,
-        bool(inverse and normalize_inverse),
-        out_t.vdx_code,
-        _compute_code(out_t, compute),
-        _signal(input_signal_range, N),
-    )
+    args = (buffer_shape, ax, kind, inverse, bool(inverse and normalize_inverse), out_t.vdx_code,
+            _compute_code(out_t, compute), _signal(input_signal_range, N))
+    plan = P.get_plan(*args)
+    _plain_args[memo_key] = args
     if print_shader:
         print(plan.describe())
     ptr = buf.ptr

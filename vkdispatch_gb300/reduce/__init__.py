@@ -173,6 +173,8 @@ class ReduceFunction:
         self.map_func = mapping_function
         self.out_type = mapping_function.return_type if mapping_function is not None else None
         self._map_code = None
+        # (input type, shape) -> validated launch layout of a call
+        self._layouts = {}
 
     def _resolve_map(self, in_type: dt.dtype) -> int:
         if self.map_func is None:
@@ -183,6 +185,25 @@ class ReduceFunction:
 
     def __call__(self, *args, graph: Optional[G.CommandGraph] = None, **kwargs) -> Buffer:
         src = args[0]
+        lay = self._layouts.get((src.var_type, src.shape))
+        if lay is None:
+            lay = self._layouts[(src.var_type, src.shape)] = self._layout(src)
+        map_code, n, batch, out_type, shape = lay
+        res = Buffer._empty(shape, out_type)
+        op = self.reduction.code
+        in_code = src.var_type.vdx_code
+        ptr, out = src.ptr, res.ptr
+        ws = out + batch * out_type.item_size
+
+        def launch(stream):
+            L.check(L.lib().vdx_reduce(op, map_code, in_code, ptr, n, batch, out, ws, stream), "reduce")
+
+        G.resolve(graph).record(launch, (src, res))
+        return res
+
+    def _layout(self, src):
+        """Checks a call's input and derives (map code, n, batch, output type,
+        output shape)."""
         in_type = src.var_type
         if in_type.vdx_code is None or in_type.vdx_code in (L.VDX_C32, L.VDX_C128, L.VDX_BF16X2):
             raise NotImplementedError(f"reductions over {in_type.name} buffers are not in the supported menu")
@@ -217,17 +238,7 @@ class ReduceFunction:
             L.check(L.lib().vdx_reduce_partial_count(n, ctypes.byref(parts)), "reduce")
             nparts = _partial_counts[n] = int(parts.value)
         shape = (nparts + 1,) + ((batch,) if batch > 1 else ())
-        res = Buffer(shape, out_type)
-        op = self.reduction.code
-        in_code = in_type.vdx_code
-        ptr, out = src.ptr, res.ptr
-        ws = out + batch * out_type.item_size
-
-        def launch(stream):
-            L.check(L.lib().vdx_reduce(op, map_code, in_code, ptr, n, batch, out, ws, stream), "reduce")
-
-        G.resolve(graph).record(launch, (src, res))
-        return res
+        return map_code, n, batch, out_type, shape
 
 
 def reduce(identity, axes=None, group_size=None, mapping_function: MappingFunction = None):
