@@ -457,7 +457,8 @@ __device__ __forceinline__ void store_output(const Plan& P, const Place<STRIDED>
 // IW: multiply each input point by in_weight[element] * in_weight_scale as it
 // is loaded (the 2 w y of a weighted |y|^2 loss's gradient).
 // LOSS: write one partial of sum(loss_weight[element] * |output|^2) per CTA.
-// Plans of 32 points per thread run CTAs of at most 256 threads, two per SM.
+// Plans of 32 points per thread run CTAs of at most 256 threads with up to
+// 128 registers per thread.
 template <class Plan, bool INV, bool STRIDED, class S, class Re, int IW = 0, int LOSS = 0>
 __global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 32 ? 2 : 1) k_c2c(FftArgs a) {
   const Plan P(a.pp);
@@ -585,16 +586,13 @@ __global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 3
   store_output<Plan, true, S, Re>(P, pl, a, v);
 }
 
-// Strided fused convolution for CTAs of at most 256 threads, complex64 (two
-// CTAs per SM with 16 or 32 points per thread, three with 8).  Plans of up
-// to 16 points per thread hold the kernel spectrum in registers from the
-// start; with 32 the registers are full and it is loaded after the forward
-// FFT.
-// The signal loads are issued first and the kernel-spectrum loads right
-// after them, into registers, so the kernel spectrum's HBM latency overlaps
-// the forward passes instead of following them (the registers it takes need
-// the 256-thread launch bound).  The kernel spectrum is read once, with
-// evict-first loads.
+// Strided fused convolution for CTAs of at most 256 threads, complex64.  The
+// launch bound allows 128 registers per thread (80 for plans of 8 points
+// per thread).  Plans of up to 16 points per thread load the kernel
+// spectrum into registers right after issuing the signal loads, so its HBM
+// latency overlaps the forward passes instead of following them; with 32
+// points per thread the registers are full and it is loaded after the
+// forward FFT.  The kernel spectrum is read once, with evict-first loads.
 template <class Plan, class S, class Re, int KOP>
 __global__ void __launch_bounds__(256, Plan::MAXE <= 8 ? 3 : 2) k_conv_pf(FftArgs a) {
   const Plan P(a.pp);
