@@ -131,3 +131,29 @@ def test_fused_loss_finite_differences_fp64():
                 fd.append((lp - lm) / (2 * eps))
             fd = fd[0] + 1j * fd[1]  # PyTorch convention: dL/dRe + i dL/dIm
             assert abs(grad[idx] - fd) <= 1e-4 * max(1.0, abs(fd)), (which, idx, grad[idx], fd)
+
+
+@pytest.mark.parametrize("shape", [(6, 512), (4, 1024), (512, 6)])
+def test_fused_loss_on_two_pass_plans(monkeypatch, shape):
+    """The fused loss and its adjoints (spectrum-saving and kernel-gradient
+    convolution variants, weighted-|y|^2 partials) on the two-pass radix-32
+    compile-time plans of 512 and 1024 points."""
+    from vkdispatch_gb300.fft import plan as P
+
+    monkeypatch.setenv("VDX_POINTS_PER_THREAD", "32")
+    P.cache_clear()
+    x64 = crand(shape, 5)
+    k64 = crand(shape, 6, 0.1)
+    g = torch.Generator().manual_seed(7)
+    w64 = torch.rand(shape, generator=g, dtype=torch.float64)
+    xr, kr = x64.cuda().requires_grad_(True), k64.cuda().requires_grad_(True)
+    lr, _ = _torch_loss(xr, kr, w64.cuda())
+    lr.backward()
+    xa = x64.to(torch.complex64).cuda().requires_grad_(True)
+    ka = k64.to(torch.complex64).cuda().requires_grad_(True)
+    loss = ag.conv_weighted_sqnorm(xa, ka, w64.float().cuda())
+    loss.backward()
+    assert abs(loss.item() - lr.item()) / abs(lr.item()) < 1e-5
+    assert rel_l2(xa.grad.cpu().numpy(), xr.grad.cpu().numpy()) < 1e-5
+    assert rel_l2(ka.grad.cpu().numpy(), kr.grad.cpu().numpy()) < 1e-5
+    P.cache_clear()

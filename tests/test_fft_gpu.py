@@ -323,10 +323,12 @@ def test_strided_convolution_points_per_thread(monkeypatch, kop_conj, pts):
     P.cache_clear()
 
 
-@pytest.mark.parametrize("shape,axis", [((96, 1024), 1), ((1024, 40), 0), ((3, 1024, 5), 1)])
-def test_c2c_1024_two_pass_plan(monkeypatch, shape, axis):
-    """The radix 32 x 32 compile-time plan (one warp per 1024-point
-    transform) matches FP64 numpy forward and inverse, contiguous and strided."""
+@pytest.mark.parametrize("shape,axis", [((96, 1024), 1), ((1024, 40), 0), ((3, 1024, 5), 1), ((70, 512), 1),
+                                        ((512, 33), 0)])
+def test_c2c_two_pass_plans(monkeypatch, shape, axis):
+    """The two-pass compile-time plans (radix 32 x 32, one warp per
+    1024-point transform; radix 32 x 16 for 512 points) match FP64 numpy
+    forward and inverse, contiguous and strided."""
     import torch
 
     from vkdispatch_gb300 import _lib as L
@@ -340,15 +342,17 @@ def test_c2c_1024_two_pass_plan(monkeypatch, shape, axis):
     s = torch.cuda.current_stream().cuda_stream
     fwd = P.get_plan(shape, axis, L.VDX_KIND_C2C, False, False, L.VDX_C64, L.VDX_C64)
     d = fwd.describe()
-    assert d["threads_per_transform"] == 32 and d["radices"] == "32x32" and d["fixed"] is True
+    n = shape[axis]
+    assert d["threads_per_transform"] == n // 32 and d["fixed"] is True
+    assert d["radices"] == {512: "32x16", 1024: "32x32"}[n]
     fwd.exec(t.data_ptr(), t.data_ptr(), None, s)
     torch.cuda.synchronize()
     ref = np.fft.fft(x.astype(np.complex128), axis=axis)
-    assert rel_l2(t.cpu().numpy(), ref) <= tol_fp32(1024)
+    assert rel_l2(t.cpu().numpy(), ref) <= tol_fp32(n)
     inv = P.get_plan(shape, axis, L.VDX_KIND_C2C, True, True, L.VDX_C64, L.VDX_C64)
     inv.exec(t.data_ptr(), t.data_ptr(), None, s)
     torch.cuda.synchronize()
-    assert rel_l2(t.cpu().numpy(), x) <= 2 * tol_fp32(1024)
+    assert rel_l2(t.cpu().numpy(), x) <= 2 * tol_fp32(n)
     P.cache_clear()
 
 
