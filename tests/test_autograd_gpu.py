@@ -157,3 +157,18 @@ def test_fused_loss_on_two_pass_plans(monkeypatch, shape):
     assert rel_l2(xa.grad.cpu().numpy(), xr.grad.cpu().numpy()) < 1e-5
     assert rel_l2(ka.grad.cpu().numpy(), kr.grad.cpu().numpy()) < 1e-5
     P.cache_clear()
+
+
+def test_lazy_conjugate_and_negative_views():
+    """conj() and neg() views (PyTorch's lazy bits, raw memory unchanged) are
+    resolved before the kernels read memory, in the forward and the backward."""
+    x = crand((8, 64), 21).to(torch.complex64).cuda()
+    got = ag.fft(x.conj())
+    assert rel_l2(got.cpu().numpy(), torch.fft.fft(x.conj()).cpu().numpy()) < 1e-6
+    got = ag.fft(torch.neg(x.conj()))
+    assert rel_l2(got.cpu().numpy(), torch.fft.fft(-x.conj()).cpu().numpy()) < 1e-6
+    xa = x.clone().requires_grad_(True)
+    xr = x.clone().requires_grad_(True)
+    (ag.ifft(xa).conj().real.sum() + ag.fft(xa).conj().imag.sum()).backward()
+    (torch.fft.ifft(xr).conj().real.sum() + torch.fft.fft(xr).conj().imag.sum()).backward()
+    assert rel_l2(xa.grad.cpu().numpy(), xr.grad.cpu().numpy()) < 1e-6

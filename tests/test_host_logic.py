@@ -199,3 +199,22 @@ def test_multi_kernel_map_strides_are_recognised():
     assert vd.fft.mapped_kernel_index() is None
     with pytest.raises(NotImplementedError):
         M.classify_output(vd.map(bad))
+
+
+def test_torch_fft_front_end_norm_codes_and_cpu_refusal():
+    """torch.fft norm modes map to libvdx normalize codes (0 none, 1 1/n,
+    2 1/sqrt(n)) per direction; CPU tensors are refused, with no fallback."""
+    import torch
+
+    import vkdispatch_gb300.torch_fft as tf
+
+    assert tf._norm_code(None, False) == 0 and tf._norm_code(None, True) == 1
+    assert tf._norm_code("backward", False) == 0 and tf._norm_code("backward", True) == 1
+    assert tf._norm_code("forward", False) == 1 and tf._norm_code("forward", True) == 0
+    assert tf._norm_code("ortho", False) == 2 and tf._norm_code("ortho", True) == 2
+    with pytest.raises(ValueError):
+        tf._norm_code("none", False)
+    with pytest.raises(ValueError):
+        tf.fft(torch.zeros(8, dtype=torch.complex64))
+    dims, sizes = tf._dims(torch.zeros(2, 3, 4), (5, 6), None)
+    assert dims == (1, 2) and sizes == (5, 6)

@@ -13,6 +13,7 @@ provides device memory and streams.  There is no CPU fallback.
 from . import codegen  # noqa: F401
 from . import fft  # noqa: F401
 from . import reduce  # noqa: F401
+from . import torch_fft  # noqa: F401
 from ._lib import lib as _load_lib  # noqa: F401
 from .buffer import Buffer, RFFTBuffer, asbuffer, asrfftbuffer, from_cuda_array  # noqa: F401
 from .dtypes import (  # noqa: F401

@@ -37,6 +37,12 @@ def _stream() -> int:
     return G.current_stream_handle()
 
 
+def _raw(t: torch.Tensor) -> torch.Tensor:
+    """t with PyTorch's lazy conjugate / negative views applied and C-contiguous:
+    the kernels read raw memory, which a conj() or neg() view does not change."""
+    return t.resolve_conj().resolve_neg().contiguous()
+
+
 def _check_tensor(t: torch.Tensor, name: str) -> None:
     if not t.is_cuda:
         raise ValueError(f"{name} must be a CUDA tensor (there is no CPU path)")
@@ -44,9 +50,21 @@ def _check_tensor(t: torch.Tensor, name: str) -> None:
         raise ValueError(f"{name} must be C-contiguous")
 
 
+def smooth13(n: int) -> bool:
+    """True when n has no prime factor above 13 (the radix kernels' lengths)."""
+    for p in (2, 3, 5, 7, 11, 13):
+        while n % p == 0:
+            n //= p
+    return n == 1
+
+
 def _c2c_plan(shape, axis, inverse, scale_1n, dtype):
+    # lengths with larger prime factors run as Bluestein transforms; the flag
+    # is explicit so that the backward pass (on autograd's own thread) plans
+    # the same way as the forward
     io, comp = _IO[dtype]
-    return P.get_plan(tuple(shape), axis, L.VDX_KIND_C2C, inverse, scale_1n, io, comp)
+    flags = None if smooth13(int(shape[axis])) else L.VDX_FFT_FLAG_BLUESTEIN
+    return P.get_plan(tuple(shape), axis, L.VDX_KIND_C2C, inverse, scale_1n, io, comp, flags=flags)
 
 
 def _conv_plan(shape, axis, kop, dtype):
@@ -65,6 +83,7 @@ def _ops(**kw) -> L.ExecOps:
 # C2C transforms
 # ---------------------------------------------------------------------------
 def _c2c(x: torch.Tensor, dim: int, inverse: bool, scale_1n: bool) -> torch.Tensor:
+    x = _raw(x)
     _check_tensor(x, "input")
     if x.dtype not in _IO:
         raise ValueError("complex64 or complex128 input required")
@@ -78,12 +97,12 @@ class FFTFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, dim: int, inverse: bool, scale_1n: bool):
         ctx.cfg = (dim, inverse, scale_1n)
-        return _c2c(x.contiguous(), dim, inverse, scale_1n)
+        return _c2c(_raw(x), dim, inverse, scale_1n)
 
     @staticmethod
     def backward(ctx, g):
         dim, inverse, scale_1n = ctx.cfg
-        return _c2c(g.contiguous(), dim, not inverse, scale_1n), None, None, None
+        return _c2c(_raw(g), dim, not inverse, scale_1n), None, None, None
 
 
 def fft(x: torch.Tensor, dim: int = -1) -> torch.Tensor:
@@ -116,7 +135,7 @@ def _rfft_raw(x: torch.Tensor) -> torch.Tensor:
 
 
 def _irfft_raw(h: torch.Tensor, n: int, scale_1n: bool) -> torch.Tensor:
-    buf = h.contiguous().clone()
+    buf = _raw(h).clone()
     io, comp = _IO[h.dtype]
     shape = tuple(h.shape[:-1]) + (n,)
     P.get_plan(shape, len(shape) - 1, L.VDX_KIND_C2R, True, scale_1n, io, comp).exec(
@@ -132,14 +151,15 @@ def _interior(n: int) -> slice:
 class RFFTFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x):
+        x = _raw(x)
         _check_tensor(x, "input")
         ctx.n = x.shape[-1]
-        return _rfft_raw(x.contiguous())
+        return _rfft_raw(x)
 
     @staticmethod
     def backward(ctx, g):
         n = ctx.n
-        h = g.contiguous().clone()
+        h = _raw(g).clone()
         h[..., _interior(n)] *= 0.5
         return _irfft_raw(h, n, scale_1n=False)
 
@@ -147,6 +167,7 @@ class RFFTFunction(torch.autograd.Function):
 class IRFFTFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, h, n: int):
+        h = _raw(h)
         _check_tensor(h, "input")
         ctx.n = n
         return _irfft_raw(h, n, scale_1n=True)
@@ -154,7 +175,7 @@ class IRFFTFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g):
         n = ctx.n
-        gh = _rfft_raw(g.contiguous())
+        gh = _rfft_raw(_raw(g))
         gh[..., _interior(n)] *= 2.0
         return gh / n, None
 
@@ -230,6 +251,7 @@ def _conv_backward(g, spec, khat, w=None, grad_loss=None):
 class FFTConvFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, khat):
+        x, khat = _raw(x), _raw(khat)
         for t, nm in ((x, "x"), (khat, "khat")):
             _check_tensor(t, nm)
         if x.dtype != torch.complex64 or khat.dtype != torch.complex64 or khat.shape != x.shape:
@@ -241,7 +263,7 @@ class FFTConvFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g):
         spec, khat = ctx.saved_tensors
-        gx, gk = _conv_backward(g.contiguous(), spec, khat)
+        gx, gk = _conv_backward(_raw(g), spec, khat)
         return gx, gk
 
 
@@ -253,6 +275,7 @@ def fft_convolve(x: torch.Tensor, khat: torch.Tensor) -> torch.Tensor:
 class ConvWeightedSqnormFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, khat, w):
+        x, khat, w = _raw(x), _raw(khat), _raw(w)
         for t, nm in ((x, "x"), (khat, "khat"), (w, "w")):
             _check_tensor(t, nm)
         if x.dim() < 2:
