@@ -197,6 +197,22 @@ typedef struct vdx_exec_ops {
 int vdx_fft_exec_ops(const vdx_plan* plan, const void* in, void* out, const void* kernel, const vdx_exec_ops* ops,
                      void* stream);
 
+/*
+ * One signal convolved with kernel_num kernels in one launch (the reference's
+ * kernel_num > 1 convolution shader, vkdispatch/fft/shader_factories.py:
+ * 166-193, and the kernel_num argument of vd.fft.convolve, vkdispatch/fft/
+ * functions.py:476-547): kernel k is read at kernel + k * kernel_stride and
+ * output slice k written at out + k * out_stride (strides in elements of the
+ * plan's storage type).  The signal is read and transformed once.  `in` must
+ * not overlap the output slices of other transforms.  Returns
+ * VDX_ERR_UNSUPPORTED for plans without a fused kernel (long four-step axes,
+ * Bluestein lengths, the alternative compile-time plans, 4-byte storage, or
+ * when the spectrum does not fit in shared memory); the caller then runs one
+ * vdx_fft_exec per kernel.
+ */
+int vdx_conv_exec_multi(const vdx_plan* plan, const void* in, void* out, const void* kernel, int kernel_num,
+                        int64_t kernel_stride, int64_t out_stride, void* stream);
+
 /* Number of CTAs one vdx_fft_exec of this plan launches. */
 int vdx_fft_plan_ctas(const vdx_plan* plan, int64_t* ctas);
 

@@ -92,3 +92,51 @@ def test_unrecognised_index_expression_is_refused():
     b = vd.Buffer((2, 32), vd.complex64)
     with pytest.raises(NotImplementedError):
         vd.fft.convolve(b, b, vd.Buffer((4, 32), vd.complex64), kernel_map=vd.map(bad_map), kernel_num=2)
+
+
+@pytest.mark.parametrize("dtype,axis", [("complex64", 1), ("complex64", 0), ("complex128", 1)])
+def test_fused_multi_kernel_launch(dtype, axis):
+    """One launch for all kernels (vdx_conv_exec_multi) against one
+    convolution launch per kernel and FP64 numpy."""
+    import torch
+
+    from vkdispatch_gb300 import _lib as L
+    from vkdispatch_gb300.fft import plan as P
+
+    rng = np.random.default_rng(30 + axis)
+    B, N, K = 8, 384, 4
+    shape = (B, N) if axis == 1 else (N, B)
+    tdt = getattr(torch, dtype)
+    code = L.VDX_C64 if dtype == "complex64" else L.VDX_C128
+    x = crandn(rng, shape).astype(dtype)
+    bank = (crandn(rng, (K,) + shape) * 0.1).astype(dtype)
+    xt, kt = torch.from_numpy(x).cuda(), torch.from_numpy(bank).cuda()
+    slab = B * N
+    plan = P.get_plan(shape, axis, L.VDX_KIND_CONV, False, True, code, code, None, L.VDX_KOP_MUL_CONJ, code)
+    s = torch.cuda.current_stream().cuda_stream
+    fused = torch.empty((K,) + shape, dtype=tdt, device="cuda")
+    assert plan.exec_multi(xt.data_ptr(), fused.data_ptr(), kt.data_ptr(), K, slab, slab, s)
+    loop = torch.empty_like(fused)
+    for k in range(K):
+        plan.exec(xt.data_ptr(), loop[k].data_ptr(), kt[k].data_ptr(), s)
+    torch.cuda.synchronize()
+    assert rel_l2(fused.cpu().numpy(), loop.cpu().numpy()) <= (1e-6 if dtype == "complex64" else 1e-14)
+    spec = np.fft.fft(x.astype(np.complex128), axis=axis)
+    tol = 2 * tol_fp32(N) if dtype == "complex64" else 1e-12
+    for k in range(K):
+        ref = np.fft.ifft(spec * np.conj(bank[k]), axis=axis)
+        assert rel_l2(fused[k].cpu().numpy(), ref) <= tol
+    assert rel_l2(xt.cpu().numpy(), x) == 0.0  # the signal is not modified
+
+
+def test_fused_multi_kernel_refuses_plans_without_a_fused_kernel():
+    import torch
+
+    from vkdispatch_gb300 import _lib as L
+    from vkdispatch_gb300.fft import plan as P
+
+    c = L.VDX_C32
+    plan = P.get_plan((4, 256), 1, L.VDX_KIND_CONV, False, True, c, L.VDX_C64, None, L.VDX_KOP_MUL_CONJ, c)
+    buf = torch.zeros((2, 4, 256, 2), dtype=torch.float16, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    assert plan.exec_multi(buf.data_ptr(), buf.data_ptr(), buf.data_ptr(), 2, 0, 1024, s) is False

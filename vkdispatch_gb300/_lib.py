@@ -50,6 +50,7 @@ EXPORTED = (
     "vdx_fft_exec_ops",
     "vdx_fft_plan_ctas",
     "vdx_convert",
+    "vdx_conv_exec_multi",
     "vdx_batch_plan_create",
     "vdx_batch_plan_destroy",
     "vdx_batch_plan_describe",
@@ -138,6 +139,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.vdx_fft_plan_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     lib.vdx_convert.restype = i32
     lib.vdx_convert.argtypes = [vp, i32, vp, i32, i64, vp]
+    lib.vdx_conv_exec_multi.restype = i32
+    lib.vdx_conv_exec_multi.argtypes = [vp, vp, vp, vp, i32, i64, i64, vp]
     lib.vdx_batch_plan_create.restype = i32
     lib.vdx_batch_plan_create.argtypes = [ctypes.POINTER(BatchItem), i32, i32, i32, ctypes.POINTER(vp)]
     lib.vdx_batch_plan_destroy.restype = i32

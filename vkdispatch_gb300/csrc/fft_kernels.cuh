@@ -435,11 +435,13 @@ __device__ __forceinline__ void gather_input(const Plan& P, const Place<STRIDED>
   }
 }
 
-// Natural-order store of the last executed pass, scaled.
+// Natural-order store of the last executed pass, scaled, to `base` (a.out
+// unless given) at the thread's transform offset.
 template <class Plan, bool REV, class S, class Re, bool STRIDED>
-__device__ __forceinline__ void store_output(const Plan& P, const Place<STRIDED>& pl, const FftArgs& a, Cx<Re>* v) {
+__device__ __forceinline__ void store_output(const Plan& P, const Place<STRIDED>& pl, const FftArgs& a, Cx<Re>* v,
+                                             S* base = nullptr) {
   constexpr int MAXE = Plan::MAXE;
-  S* out = reinterpret_cast<S*>(a.out) + pl.out0();
+  S* out = (base ? base : reinterpret_cast<S*>(a.out)) + pl.out0();
   const int n = P.n();
   const Re s = Re(a.scale);
   const bool all = pl.tile_full;
@@ -642,6 +644,61 @@ __global__ void __launch_bounds__(256, Plan::MAXE <= 8 ? 3 : 2) k_conv_pf(FftArg
   });
   P.template run<true, true>(v, pl, sm, tw);
   store_output<Plan, true, S, Re>(P, pl, a, v);
+}
+
+// Fused multi-kernel convolution (the reference's kernel_num > 1 shader,
+// vkdispatch/fft/shader_factories.py:166-193): the signal is read and
+// transformed once, then for each kernel k: * K_k (conjugate or plain
+// product) -> inverse FFT -> output slice k.  Kernel k is read at
+// a.ker + k * kstride and output slice k written at a.out + k * ostride
+// (elements).  The forward spectrum waits in a thread-private region at the
+// end of the dynamic shared memory (slot i * blockDim.x + threadIdx.x, MAXE
+// slots per thread), so only the exchange region is shared between threads.
+template <class Plan, bool STRIDED, class S, class Re, int KOP>
+__global__ void __launch_bounds__(1024) k_conv_multi(FftArgs a, int K, long long kstride, long long ostride) {
+  const Plan P(a.pp);
+  constexpr int MAXE = Plan::MAXE;
+  const Place<STRIDED> pl(a, P.T());
+  Cx<Re>* sm = smem_base<Re>();
+  const Cx<Re>* tw = reinterpret_cast<const Cx<Re>*>(a.tw);
+  unsigned dyn;
+  asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+  Cx<Re>* keep = sm + (dyn / sizeof(Cx<Re>) - unsigned(MAXE) * blockDim.x);
+  const S* in = reinterpret_cast<const S*>(a.in) + pl.in0();
+  Cx<Re> v[MAXE];
+  P.assume_t(pl.t);
+  const int n = P.n();
+  gather_input<Plan, S, Re>(P, pl, a, v, in);
+  const bool kvalid = pl.tile_full || pl.valid;
+  P.template run<false, false>(v, pl, sm, tw);
+#pragma unroll
+  for (int i = 0; i < MAXE; ++i) keep[i * blockDim.x + threadIdx.x] = v[i];
+  for (int k = 0; k < K; ++k) {
+    if (k > 0) {
+#pragma unroll
+      for (int i = 0; i < MAXE; ++i) v[i] = keep[i * blockDim.x + threadIdx.x];
+    }
+    const S* ker = reinterpret_cast<const S*>(a.ker) + k * kstride + pl.ker0();
+    P.template last<false>([&](auto rc) {
+      constexpr int RR = decltype(rc)::value;
+      constexpr int B = MAXE / RR;
+      const int nb = n / RR;
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        const int j = pl.t + b * P.T();
+        if (j < nb) {
+#pragma unroll
+          for (int r = 0; r < RR; ++r) {
+            const int pos = j + r * nb;
+            const Cx<Re> kv = kvalid ? Conv<S, Re>::ld(ker + pos * pl.ps) : mk<Re>(Re(0), Re(0));
+            v[b * RR + r] = KOP == 0 ? cmulc(v[b * RR + r], kv) : cmul(v[b * RR + r], kv);
+          }
+        }
+      }
+    });
+    P.template run<true, true>(v, pl, sm, tw);
+    store_output<Plan, true, S, Re>(P, pl, a, v, reinterpret_cast<S*>(a.out) + k * ostride);
+  }
 }
 
 // ---------------------------------------------------------------------------

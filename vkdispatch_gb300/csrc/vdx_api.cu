@@ -1340,6 +1340,39 @@ int vdx_fft_exec_ops(const vdx_plan* p, const void* in, void* out, const void* k
   return exec_plan(p, in, out, kernel, ops, stream);
 }
 
+int vdx_conv_exec_multi(const vdx_plan* p, const void* in, void* out, const void* kernel, int kernel_num,
+                        int64_t kernel_stride, int64_t out_stride, void* stream) {
+  if (!p) return fail(VDX_ERR_INVALID, "plan is NULL");
+  if (!in || !out || !kernel) return fail(VDX_ERR_INVALID, "in, out and kernel must be non-NULL device pointers");
+  if (kernel_num < 1 || kernel_stride < 0 || out_stride < 0)
+    return fail(VDX_ERR_INVALID, "kernel_num must be >= 1 and the strides >= 0");
+  if (p->op != OP_CONV) return fail(VDX_ERR_INVALID, "vdx_conv_exec_multi needs a convolution plan");
+  if (p->fourstep || p->bluestein || p->fixed_pts || (p->store != ST_C64 && p->store != ST_C128))
+    return fail(VDX_ERR_UNSUPPORTED, "no fused multi-kernel kernel for this plan (run one convolution per kernel)");
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev != p->dev) return fail(VDX_ERR_INVALID, "plan was created on another device");
+  FftArgs a = p->args;
+  a.in = in;
+  a.out = out;
+  a.ker = kernel;
+  Launch l = p->launch;
+  l.stream = reinterpret_cast<cudaStream_t>(stream);
+  // the exchange region, then MAXE complex slots per thread for the spectrum
+  const size_t cbytes = p->f64 ? 16 : 8;
+  l.smem = ((l.smem + 15) & ~size_t(15)) + size_t(conv_multi_points(p->f64)) * l.block.x * cbytes;
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (l.smem > size_t(optin))
+    return fail(VDX_ERR_UNSUPPORTED, "the multi-kernel spectrum does not fit in shared memory (run one convolution "
+                                     "per kernel)");
+  e = launch_conv_multi(p->store, p->strided, a, l, p->d.kernel_op, kernel_num, (long long)kernel_stride,
+                        (long long)out_stride);
+  if (e != cudaSuccess) return cuda_fail(e, "multi-kernel convolution launch");
+  return VDX_OK;
+}
+
 int vdx_fft_plan_ctas(const vdx_plan* p, int64_t* ctas) {
   if (!p || !ctas) return fail(VDX_ERR_INVALID, "plan and ctas must be non-NULL");
   *ctas = (int64_t)p->launch.grid.x;

@@ -124,6 +124,12 @@ cudaError_t launch_fixedpts_conv_c64(int pts, const FftArgs& a, const Launch& l,
 template <int N>
 cudaError_t launch_fixed32_c64(const FftArgs& a, const Launch& l, int op, bool strided, int kop, int variant);
 bool has_fixedpts_c64(int n, int pts, bool conv, bool strided);
+
+// fused multi-kernel convolution on the runtime-plan kernels (ST_C64 or
+// ST_C128 storage); conv_multi_points = the kernel's points per thread
+cudaError_t launch_conv_multi(int store, bool strided, const FftArgs& a, const Launch& l, int kop, int K,
+                              long long kstride, long long ostride);
+int conv_multi_points(bool f64);
 cudaError_t launch_fixedpts_c64_any(int n, int pts, const FftArgs& a, const Launch& l, int op, bool strided, int kop,
                                     int variant);
 

@@ -524,9 +524,11 @@ def _convolve_multi(buffers, kernel_map, kernel_num, buffer_shape, graph, axis, 
     166-193): for kernel k the kernel map reads, and the output map writes,
     ``io_index + mapped_kernel_index() * C`` -- C * k elements along their
     buffers (C = 0 when the map does not use the index).  One fused
-    convolution launch per kernel; the signal is read from a copy when an
-    output slice overlaps it, so every kernel sees the original signal, as in
-    the reference's single pass over the input."""
+    convolution launch for all kernels (the signal read and transformed
+    once) where the plan has such a kernel, else one fused convolution launch
+    per kernel; the signal is read from a copy when an output slice overlaps
+    it, so every kernel sees the original signal, as in the reference's
+    single pass over the input."""
     import torch
 
     from . import maps as M
@@ -585,6 +587,8 @@ def _convolve_multi(buffers, kernel_map, kernel_num, buffer_shape, graph, axis, 
         if stage is not None:
             L.convert(in_ptr, code, stage.data_ptr(), code, total, s)
             src = stage.data_ptr()
+        if plan.exec_multi(src, out_ptr, k_ptr, kernel_num, kstride, ostride, s):
+            return
         for k in range(kernel_num):
             plan.exec(src, out_ptr + k * ostride * es, k_ptr + k * kstride * es, s)
 

@@ -94,6 +94,17 @@ class Plan:
     def exec(self, in_ptr: int, out_ptr: int, ker_ptr: Optional[int], stream: int) -> None:
         L.check(L.lib().vdx_fft_exec(self.handle, in_ptr, out_ptr, ker_ptr, stream), "FFT exec")
 
+    def exec_multi(self, in_ptr: int, out_ptr: int, ker_ptr: int, kernel_num: int, kernel_stride: int,
+                   out_stride: int, stream: int) -> bool:
+        """One launch for kernel_num kernels (strides in elements); False when
+        the plan has no fused multi-kernel kernel (nothing was launched)."""
+        rc = L.lib().vdx_conv_exec_multi(self.handle, in_ptr, out_ptr, ker_ptr, kernel_num, kernel_stride,
+                                         out_stride, stream)
+        if rc == L.VDX_ERR_UNSUPPORTED:
+            return False
+        L.check(rc, "multi-kernel convolution")
+        return True
+
     def exec_ops(self, in_ptr: int, out_ptr: int, ker_ptr: Optional[int], ops: L.ExecOps, stream: int) -> None:
         L.check(L.lib().vdx_fft_exec_ops(self.handle, in_ptr, out_ptr, ker_ptr, ctypes.byref(ops), stream),
                 "FFT exec")
