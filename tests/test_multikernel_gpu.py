@@ -94,17 +94,19 @@ def test_unrecognised_index_expression_is_refused():
         vd.fft.convolve(b, b, vd.Buffer((4, 32), vd.complex64), kernel_map=vd.map(bad_map), kernel_num=2)
 
 
-@pytest.mark.parametrize("dtype,axis", [("complex64", 1), ("complex64", 0), ("complex128", 1)])
-def test_fused_multi_kernel_launch(dtype, axis):
-    """One launch for all kernels (vdx_conv_exec_multi) against one
-    convolution launch per kernel and FP64 numpy."""
+@pytest.mark.parametrize("dtype,axis,N", [("complex64", 1, 384), ("complex64", 0, 384), ("complex128", 1, 384),
+                                          ("complex64", 1, 1024), ("complex64", 0, 512)])
+def test_fused_multi_kernel_launch(dtype, axis, N):
+    """One launch for all kernels (vdx_conv_exec_multi; runtime-radix and
+    compile-time plans) against one convolution launch per kernel and FP64
+    numpy."""
     import torch
 
     from vkdispatch_gb300 import _lib as L
     from vkdispatch_gb300.fft import plan as P
 
     rng = np.random.default_rng(30 + axis)
-    B, N, K = 8, 384, 4
+    B, K = 8, 4
     shape = (B, N) if axis == 1 else (N, B)
     tdt = getattr(torch, dtype)
     code = L.VDX_C64 if dtype == "complex64" else L.VDX_C128

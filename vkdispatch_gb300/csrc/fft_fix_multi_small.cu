@@ -1,0 +1,37 @@
+// Fused multi-kernel convolutions (one signal, kernel_num kernels) on the
+// compile-time complex64 plans of power-of-two lengths 16 to 512.
+#include "fft_launch.cuh"
+
+namespace vdx {
+
+namespace {
+
+template <int N>
+cudaError_t launch_fixed_multi(bool strided, const FftArgs& a, const Launch& l, int kop, int K, long long kstride,
+                               long long ostride) {
+  using Plan = Pow2Plan<N>;
+  using S = Cx<float>;
+  if (strided) {
+    if (kop == 0) return enqueue(k_conv_multi<Plan, true, S, float, 0>, l, a, K, kstride, ostride);
+    return enqueue(k_conv_multi<Plan, true, S, float, 1>, l, a, K, kstride, ostride);
+  }
+  if (kop == 0) return enqueue(k_conv_multi<Plan, false, S, float, 0>, l, a, K, kstride, ostride);
+  return enqueue(k_conv_multi<Plan, false, S, float, 1>, l, a, K, kstride, ostride);
+}
+
+}  // namespace
+
+cudaError_t launch_fixed_conv_multi_small(int n, bool strided, const FftArgs& a, const Launch& l, int kop, int K,
+                                     long long kstride, long long ostride) {
+  switch (n) {
+    case 16: return launch_fixed_multi<16>(strided, a, l, kop, K, kstride, ostride);
+    case 32: return launch_fixed_multi<32>(strided, a, l, kop, K, kstride, ostride);
+    case 64: return launch_fixed_multi<64>(strided, a, l, kop, K, kstride, ostride);
+    case 128: return launch_fixed_multi<128>(strided, a, l, kop, K, kstride, ostride);
+    case 256: return launch_fixed_multi<256>(strided, a, l, kop, K, kstride, ostride);
+    case 512: return launch_fixed_multi<512>(strided, a, l, kop, K, kstride, ostride);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace vdx

@@ -1347,12 +1347,7 @@ int vdx_conv_exec_multi(const vdx_plan* p, const void* in, void* out, const void
   if (kernel_num < 1 || kernel_stride < 0 || out_stride < 0)
     return fail(VDX_ERR_INVALID, "kernel_num must be >= 1 and the strides >= 0");
   if (p->op != OP_CONV) return fail(VDX_ERR_INVALID, "vdx_conv_exec_multi needs a convolution plan");
-  // the fused kernel runs the runtime-radix passes: where the plan has a
-  // compile-time kernel, one launch of it per kernel measured faster (e.g.
-  // 8 kernels over 512 x 1024 points: 0.087 ms against 0.097 ms; over
-  // 1024 x 384 points, a runtime-radix length, the fused launch took 0.095 ms
-  // against 0.140 ms)
-  if (p->fourstep || p->bluestein || p->fixed || p->fixed_pts || (p->store != ST_C64 && p->store != ST_C128))
+  if (p->fourstep || p->bluestein || p->fixed_pts || (p->store != ST_C64 && p->store != ST_C128))
     return fail(VDX_ERR_UNSUPPORTED, "no fused multi-kernel kernel for this plan (run one convolution per kernel)");
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -1372,8 +1367,16 @@ int vdx_conv_exec_multi(const vdx_plan* p, const void* in, void* out, const void
   if (l.smem > size_t(optin))
     return fail(VDX_ERR_UNSUPPORTED, "the multi-kernel spectrum does not fit in shared memory (run one convolution "
                                      "per kernel)");
-  e = launch_conv_multi(p->store, p->strided, a, l, p->d.kernel_op, kernel_num, (long long)kernel_stride,
-                        (long long)out_stride);
+  if (p->fixed) {
+    const int n = p->args.pp.n;
+    e = n <= 512 ? launch_fixed_conv_multi_small(n, p->strided, a, l, p->d.kernel_op, kernel_num,
+                                                 (long long)kernel_stride, (long long)out_stride)
+                 : launch_fixed_conv_multi_large(n, p->strided, a, l, p->d.kernel_op, kernel_num,
+                                                 (long long)kernel_stride, (long long)out_stride);
+  } else {
+    e = launch_conv_multi(p->store, p->strided, a, l, p->d.kernel_op, kernel_num, (long long)kernel_stride,
+                          (long long)out_stride);
+  }
   if (e != cudaSuccess) return cuda_fail(e, "multi-kernel convolution launch");
   return VDX_OK;
 }
