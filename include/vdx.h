@@ -206,9 +206,9 @@ int vdx_fft_exec_ops(const vdx_plan* plan, const void* in, void* out, const void
  * plan's storage type).  The signal is read and transformed once.  `in` must
  * not overlap the output slices of other transforms.  Returns
  * VDX_ERR_UNSUPPORTED for plans without a fused kernel (long four-step axes,
- * Bluestein lengths, the 8- and 32-points-per-thread plans, 4-byte storage,
- * or when the spectrum does not fit in shared memory); the caller then runs
- * one vdx_fft_exec per kernel.
+ * Bluestein lengths, the radix-8 plan, 4-byte storage, or when the spectrum
+ * does not fit in shared memory); the caller then runs one vdx_fft_exec per
+ * kernel.
  */
 int vdx_conv_exec_multi(const vdx_plan* plan, const void* in, void* out, const void* kernel, int kernel_num,
                         int64_t kernel_stride, int64_t out_stride, void* stream);

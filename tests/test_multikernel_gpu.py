@@ -142,3 +142,30 @@ def test_fused_multi_kernel_refuses_plans_without_a_fused_kernel():
     buf = torch.zeros((2, 4, 256, 2), dtype=torch.float16, device="cuda")
     s = torch.cuda.current_stream().cuda_stream
     assert plan.exec_multi(buf.data_ptr(), buf.data_ptr(), buf.data_ptr(), 2, 0, 1024, s) is False
+
+
+@pytest.mark.parametrize("shape,axis", [((8, 1024), 1), ((512, 8), 0)])
+def test_fused_multi_kernel_on_two_pass_plans(monkeypatch, shape, axis):
+    import torch
+
+    from vkdispatch_gb300 import _lib as L
+    from vkdispatch_gb300.fft import plan as P
+
+    monkeypatch.setenv("VDX_POINTS_PER_THREAD", "32")
+    P.cache_clear()
+    rng = np.random.default_rng(40 + axis)
+    K = 3
+    x = crandn(rng, shape)
+    bank = crandn(rng, (K,) + shape) * 0.1
+    xt, kt = torch.from_numpy(x).cuda(), torch.from_numpy(bank).cuda()
+    c = L.VDX_C64
+    plan = P.get_plan(shape, axis, L.VDX_KIND_CONV, False, True, c, c, None, L.VDX_KOP_MUL, c)
+    assert plan.describe()["threads_per_transform"] == shape[axis] // 32
+    out = torch.empty((K,) + shape, dtype=torch.complex64, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    assert plan.exec_multi(xt.data_ptr(), out.data_ptr(), kt.data_ptr(), K, x.size, x.size, s)
+    torch.cuda.synchronize()
+    spec = np.fft.fft(x.astype(np.complex128), axis=axis)
+    for k in range(K):
+        assert rel_l2(out[k].cpu().numpy(), np.fft.ifft(spec * bank[k], axis=axis)) <= 2 * tol_fp32(shape[axis])
+    P.cache_clear()

@@ -655,7 +655,8 @@ __global__ void __launch_bounds__(256, Plan::MAXE <= 8 ? 3 : 2) k_conv_pf(FftArg
 // end of the dynamic shared memory (slot i * blockDim.x + threadIdx.x, MAXE
 // slots per thread), so only the exchange region is shared between threads.
 template <class Plan, bool STRIDED, class S, class Re, int KOP>
-__global__ void __launch_bounds__(1024) k_conv_multi(FftArgs a, int K, long long kstride, long long ostride) {
+__global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 32 ? 2 : 1)
+    k_conv_multi(FftArgs a, int K, long long kstride, long long ostride) {
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
   const Place<STRIDED> pl(a, P.T());

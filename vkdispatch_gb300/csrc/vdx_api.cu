@@ -1347,7 +1347,7 @@ int vdx_conv_exec_multi(const vdx_plan* p, const void* in, void* out, const void
   if (kernel_num < 1 || kernel_stride < 0 || out_stride < 0)
     return fail(VDX_ERR_INVALID, "kernel_num must be >= 1 and the strides >= 0");
   if (p->op != OP_CONV) return fail(VDX_ERR_INVALID, "vdx_conv_exec_multi needs a convolution plan");
-  if (p->fourstep || p->bluestein || p->fixed_pts || (p->store != ST_C64 && p->store != ST_C128))
+  if (p->fourstep || p->bluestein || p->fixed_pts == 8 || (p->store != ST_C64 && p->store != ST_C128))
     return fail(VDX_ERR_UNSUPPORTED, "no fused multi-kernel kernel for this plan (run one convolution per kernel)");
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -1361,17 +1361,18 @@ int vdx_conv_exec_multi(const vdx_plan* p, const void* in, void* out, const void
   l.stream = reinterpret_cast<cudaStream_t>(stream);
   // the exchange region, then MAXE complex slots per thread for the spectrum
   const size_t cbytes = p->f64 ? 16 : 8;
-  l.smem = ((l.smem + 15) & ~size_t(15)) + size_t(conv_multi_points(p->f64)) * l.block.x * cbytes;
+  const int pts = p->fixed_pts ? p->fixed_pts : conv_multi_points(p->f64);
+  l.smem = ((l.smem + 15) & ~size_t(15)) + size_t(pts) * l.block.x * cbytes;
   int optin = 0;
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (l.smem > size_t(optin))
     return fail(VDX_ERR_UNSUPPORTED, "the multi-kernel spectrum does not fit in shared memory (run one convolution "
                                      "per kernel)");
-  if (p->fixed) {
+  if (p->fixed || p->fixed_pts) {
     const int n = p->args.pp.n;
-    e = n <= 512 ? launch_fixed_conv_multi_small(n, p->strided, a, l, p->d.kernel_op, kernel_num,
+    e = n <= 512 ? launch_fixed_conv_multi_small(n, pts, p->strided, a, l, p->d.kernel_op, kernel_num,
                                                  (long long)kernel_stride, (long long)out_stride)
-                 : launch_fixed_conv_multi_large(n, p->strided, a, l, p->d.kernel_op, kernel_num,
+                 : launch_fixed_conv_multi_large(n, pts, p->strided, a, l, p->d.kernel_op, kernel_num,
                                                  (long long)kernel_stride, (long long)out_stride);
   } else {
     e = launch_conv_multi(p->store, p->strided, a, l, p->d.kernel_op, kernel_num, (long long)kernel_stride,

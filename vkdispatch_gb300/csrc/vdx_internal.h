@@ -132,10 +132,11 @@ cudaError_t launch_conv_multi(int store, bool strided, const FftArgs& a, const L
 int conv_multi_points(bool f64);
 // the same on the compile-time complex64 plans (n = 16 .. 512 and 1024 ..
 // 16384 in two translation units)
-cudaError_t launch_fixed_conv_multi_small(int n, bool strided, const FftArgs& a, const Launch& l, int kop, int K,
-                                          long long kstride, long long ostride);
-cudaError_t launch_fixed_conv_multi_large(int n, bool strided, const FftArgs& a, const Launch& l, int kop, int K,
-                                          long long kstride, long long ostride);
+// pts = 16 (Pow2Plan) or 32 (the two-pass plans of 512 and 1024 points)
+cudaError_t launch_fixed_conv_multi_small(int n, int pts, bool strided, const FftArgs& a, const Launch& l, int kop,
+                                          int K, long long kstride, long long ostride);
+cudaError_t launch_fixed_conv_multi_large(int n, int pts, bool strided, const FftArgs& a, const Launch& l, int kop,
+                                          int K, long long kstride, long long ostride);
 cudaError_t launch_fixedpts_c64_any(int n, int pts, const FftArgs& a, const Launch& l, int op, bool strided, int kop,
                                     int variant);
 
