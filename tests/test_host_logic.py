@@ -218,3 +218,59 @@ def test_torch_fft_front_end_norm_codes_and_cpu_refusal():
         tf.fft(torch.zeros(8, dtype=torch.complex64))
     dims, sizes = tf._dims(torch.zeros(2, 3, 4), (5, 6), None)
     assert dims == (1, 2) and sizes == (5, 6)
+
+
+def test_thread_local_state():
+    """Per-thread state, as the reference keeps its graph, builder and map op
+    thread-local (vkdispatch/base/command_graph.py:321-348, fft/io_manager.py:
+    14-15, tests/test_threading.py): graphs, plan-option contexts and map
+    tracing in one thread do not leak into another."""
+    import threading
+
+    from vkdispatch_gb300 import graph as G
+    from vkdispatch_gb300.fft import plan as P
+
+    idx = vd.reduce.mapped_io_index
+
+    def sn(b: Buff[f32]) -> f32:
+        return vc.sin(b[idx()])
+
+    def mag(b: Buff[c64]) -> f32:
+        v = b[idx()]
+        return vc.sqrt(v.real * v.real + v.imag * v.imag)
+
+    entered, release = threading.Event(), threading.Event()
+    seen = {}
+
+    def holder():
+        g = G.CommandGraph()
+        G.set_global_graph(g)
+        with vd.fft.autotune(), vd.fft.bluestein():
+            seen["holder_graph"] = G.global_graph() is g
+            entered.set()
+            release.wait(10)
+        G.set_global_graph(None)
+
+    def other():
+        entered.wait(10)
+        seen["other_graph_is_default"] = G.global_graph() is G.default_graph()
+        seen["other_tune"] = getattr(P._tls, "tune", False)
+        seen["other_bluestein"] = getattr(P._tls, "bluestein", False)
+        # concurrent tracing of different maps gives each its own result
+        seen["traces"] = [_trace_map(sn, [f32]) for _ in range(50)]
+        release.set()
+
+    results = []
+
+    def tracer():
+        results.extend(_trace_map(mag, [c64]) for _ in range(50))
+
+    th = [threading.Thread(target=holder), threading.Thread(target=other), threading.Thread(target=tracer)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join(20)
+    assert seen["holder_graph"] and seen["other_graph_is_default"]
+    assert seen["other_tune"] is False and seen["other_bluestein"] is False
+    assert seen["traces"] == [L.VDX_MAP_SIN] * 50
+    assert results == [L.VDX_MAP_ABS] * 50
