@@ -318,7 +318,7 @@ def _sum_f32(v: torch.Tensor) -> torch.Tensor:
 # ---------------------------------------------------------------------------
 def _fftn(x, inverse, dims: Sequence[int]):
     out = x
-    for i, ax in enumerate(dims):
+    for ax in dims:
         out = _c2c(out, ax, inverse, inverse)
     return out
 

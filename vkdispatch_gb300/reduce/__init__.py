@@ -226,10 +226,7 @@ class ReduceFunction:
                 raise ValueError("Reduction axes must be contiguous!")
             batch = int(np.prod([shape[i] for i in batched])) if batched else 1
             n = src.size // batch
-        out_code = in_type.vdx_code
-        out_type = in_type
-        if in_type == dt.complex64:
-            out_code, out_type = L.VDX_F32, dt.float32
+        out_type = dt.float32 if in_type == dt.complex64 else in_type
         if self.out_type is not None and self.out_type != out_type:
             raise NotImplementedError(f"map return type {self.out_type} does not match the reduction type {out_type}")
         nparts = _partial_counts.get(n)
