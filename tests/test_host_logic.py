@@ -274,3 +274,20 @@ def test_thread_local_state():
     assert seen["other_tune"] is False and seen["other_bluestein"] is False
     assert seen["traces"] == [L.VDX_MAP_SIN] * 50
     assert results == [L.VDX_MAP_ABS] * 50
+
+
+def test_torch_fft_front_end_resize():
+    """torch.fft's n / s: zero-pad or trim one dimension (host-side helper)."""
+    import torch
+
+    import vkdispatch_gb300.torch_fft as tf
+
+    x = torch.arange(12.0).reshape(3, 4)
+    assert tf._resize(x, 1, None) is x and tf._resize(x, 1, 4) is x
+    assert torch.equal(tf._resize(x, 1, 2), x[:, :2])
+    p = tf._resize(x, 0, 5)
+    assert p.shape == (5, 4) and torch.equal(p[:3], x) and torch.all(p[3:] == 0)
+    q = tf._resize(x, 1, 6)
+    assert q.shape == (3, 6) and torch.equal(q[:, :4], x) and torch.all(q[:, 4:] == 0)
+    with pytest.raises(ValueError):
+        tf._resize(x, 1, 0)
