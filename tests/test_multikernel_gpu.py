@@ -169,3 +169,23 @@ def test_fused_multi_kernel_on_two_pass_plans(monkeypatch, shape, axis):
     for k in range(K):
         assert rel_l2(out[k].cpu().numpy(), np.fft.ifft(spec * bank[k], axis=axis)) <= 2 * tol_fp32(shape[axis])
     P.cache_clear()
+
+
+@pytest.mark.parametrize("N", [96, 256])
+def test_kernel_bank_broadcast_over_batches(N):
+    """kernel_num kernels, each one slab broadcast over the signal's batches
+    (kernel_inner_only), through vd.fft.convolve's fused multi-kernel launch."""
+    rng = np.random.default_rng(50 + N)
+    B, K = 5, 3
+    x = crandn(rng, (B, N))
+    bank = crandn(rng, (K, N)) * 0.1
+    km, _ = _maps(N)  # kernel k at k * N, its slab broadcast over the batches
+    _, om = _maps(B * N)  # output slice k at k * B * N
+    sig, kb = vd.asbuffer(x), vd.asbuffer(bank)
+    out = vd.Buffer((K * B, N), vd.complex64)
+    vd.fft.convolve(out, sig, kb, kernel_map=km, output_map=om, kernel_num=K, buffer_shape=(B, N), axis=1,
+                    kernel_inner_only=True)
+    got = out.read(0).reshape(K, B, N)
+    s = np.fft.fft(x.astype(np.complex128), axis=1)
+    for k in range(K):
+        assert rel_l2(got[k], np.fft.ifft(s * np.conj(bank[k])[None, :], axis=1)) <= 2 * tol_fp32(N)
