@@ -98,3 +98,14 @@ def test_reduce_validation_without_gpu():
     assert rc == L.VDX_ERR_INVALID
     rc = lib.vdx_reduce(L.VDX_RED_ADD, L.VDX_MAP_IDENTITY, L.VDX_C64, 1, 10, 1, 1, 1, None)
     assert rc == L.VDX_ERR_INVALID and "map" in L.last_error()
+
+
+def test_multi_kernel_and_batch_validation_without_gpu():
+    """Host-side argument checks of the newer entry points return a status
+    before touching the device."""
+    lib = L.lib()
+    assert lib.vdx_conv_exec_multi(None, None, None, None, 2, 0, 0, None) == L.VDX_ERR_INVALID
+    assert "plan" in L.last_error()
+    assert lib.vdx_batch_plan_create(None, 0, 0, 1, None) == L.VDX_ERR_INVALID
+    ws = ctypes.c_size_t()
+    assert lib.vdx_batch_workspace_bytes(None, ctypes.byref(ws)) == L.VDX_ERR_INVALID
