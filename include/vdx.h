@@ -315,7 +315,8 @@ int vdx_reduce(int op, int map, int in_type, const void* in, int64_t n, int64_t 
  *     fails with VDX_ERR_UNSUPPORTED and launches nothing.
  *   - The first call on a device looks up the array's device address
  *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture.
+ *     before any stream capture.  The address is cached per device and CUDA
+ *     context, so the first call after a device reset looks it up again.
  *   - Every call shares the array, which keeps the last call's partials.
  *     Stage 1 writes every slot stage 2 reads, so nothing needs clearing, but
  *     calls that overlap on the GPU (other streams, other host threads) race

@@ -100,6 +100,22 @@ def test_reduce_validation_without_gpu():
     assert rc == L.VDX_ERR_INVALID and "map" in L.last_error()
 
 
+def test_reduce_noalloc_size_limit_without_gpu():
+    """A request whose stage-1 partials exceed the static scratch array is
+    refused before any CUDA call: dummy non-null pointers never reach a
+    device."""
+    lib = L.lib()
+    parts = ctypes.c_int64()
+    n = 4096 * 1024
+    assert lib.vdx_reduce_partial_count(n, ctypes.byref(parts)) == 0
+    batch = L.VDX_REDUCE_NOALLOC_SCRATCH_BYTES // (4 * parts.value) + 1
+    rc = lib.vdx_reduce_noalloc(L.VDX_RED_ADD, L.VDX_MAP_IDENTITY, L.VDX_F32, 1, n, batch, 1, None)
+    assert rc == L.VDX_ERR_UNSUPPORTED
+    assert "static scratch" in L.last_error()
+    # argument checks come first as well
+    assert lib.vdx_reduce_noalloc(L.VDX_RED_XOR, 0, L.VDX_F32, 1, 10, 1, 1, None) == L.VDX_ERR_INVALID
+
+
 def test_multi_kernel_and_batch_validation_without_gpu():
     """Host-side argument checks of the newer entry points return a status
     before touching the device."""

@@ -17,6 +17,7 @@
 #include <limits>
 #include <map>
 #include <mutex>
+#include <utility>
 
 namespace vdx {
 
@@ -203,25 +204,54 @@ static __device__ __align__(256) unsigned char g_reduce_scratch[VDX_REDUCE_NOALL
 namespace {
 
 std::mutex g_scratch_mu;
-std::map<int, void*> g_scratch_addr;  // device ordinal -> device address of g_reduce_scratch
+// (device ordinal, CUDA context) -> device address of g_reduce_scratch.  The
+// context is part of the key because a device reset (cudaDeviceReset, or a
+// primary-context release and re-create) reloads the module, after which an
+// address resolved in the old context is stale.
+std::map<std::pair<int, void*>, void*> g_scratch_addr;
+
+typedef int (*CtxGetCurrentFn)(void**);  // CUresult cuCtxGetCurrent(CUcontext*)
+
+// cuCtxGetCurrent, fetched once from the driver without linking libcuda.
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrentFn>(p);
+  });
+  return fn;
+}
 
 // Host code only sees a host-side stand-in under the name g_reduce_scratch;
 // its device address comes from cudaGetSymbolAddress, resolved once per
-// device with that device current (the caller's current device).
+// device and context with that device current (the caller's current device).
 cudaError_t scratch_for_current_device(void** out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
+  // Before this thread's first runtime call no context may be current yet;
+  // cudaGetSymbolAddress below makes the primary context current, and the
+  // context is read again after it.
+  void* ctx = nullptr;
+  CtxGetCurrentFn get = ctx_get_current();
+  if (get) get(&ctx);
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  auto it = g_scratch_addr.find(dev);
-  if (it != g_scratch_addr.end()) {
-    *out = it->second;
-    return cudaSuccess;
+  if (ctx) {
+    auto it = g_scratch_addr.find({dev, ctx});
+    if (it != g_scratch_addr.end()) {
+      *out = it->second;
+      return cudaSuccess;
+    }
   }
   void* p = nullptr;
   e = cudaGetSymbolAddress(&p, g_reduce_scratch);
   if (e != cudaSuccess) return e;
-  g_scratch_addr[dev] = p;
+  if (!ctx && get) get(&ctx);  // the lookup made the primary context current
+  if (ctx) g_scratch_addr[{dev, ctx}] = p;
   *out = p;
   return cudaSuccess;
 }
