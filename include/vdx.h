@@ -260,6 +260,19 @@ int vdx_batch_plan_describe(const vdx_batch_plan* plan, char* buf, size_t n);
 int vdx_batch_workspace_bytes(const vdx_batch_plan* plan, size_t* bytes);
 int vdx_batch_exec(const vdx_batch_plan* plan, void* data, void* workspace, void* stream);
 int vdx_batch_status(const vdx_batch_plan* plan, int* status);
+/*
+ * Sets the poll limit of the launch's dependency waits (default 2^22 polls of
+ * about 100 ns) and clears the plan's status word (synchronous).  A
+ * second-pass unit whose column units have not all finished after
+ * `wait_limit` polls sets the status to 1, skips its work and the launch goes
+ * on.  `extra_dependency` > 0 raises every second-pass unit's dependency
+ * count above the number of column units that exist, so those waits can only
+ * end at the limit: a host-side way to test that a wait which runs out
+ * returns a status instead of hanging (0 restores normal operation).  Not
+ * thread-safe against a concurrent vdx_batch_exec of the same plan.  No
+ * counterpart in the reference, whose kernels never wait on one another.
+ */
+int vdx_batch_plan_set_wait(vdx_batch_plan* plan, int64_t wait_limit, int32_t extra_dependency);
 
 /* reduction operations (vkdispatch/reduce/operations.py:17-66) */
 #define VDX_RED_ADD 0

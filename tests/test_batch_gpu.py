@@ -110,3 +110,49 @@ def test_autotuned_batch_plan_matches_numpy():
         err = np.linalg.norm(got[off:off + n * c].reshape(c, n) - ref) / np.linalg.norm(ref)
         assert err <= 5e-7 * max(1.0, np.log2(n)) * 2
     assert plan.status() == 0
+
+
+def test_bounded_wait_runs_out_and_reports():
+    """A dependency that can never complete (injected on the host) makes every
+    second-pass wait run out at a short poll limit: the launch returns, the
+    status word reads 1, and the same plan and another plan on the same
+    stream then run clean."""
+    items, total = pack_items([(32768, 3), (256, 4)])
+    rng = np.random.default_rng(5)
+    x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex64)
+    d = torch.from_numpy(x).cuda()
+    plan = BatchPlan(items)
+    assert plan.describe()["long_items"] == 1
+    ws = plan.make_workspace()
+    plan.set_wait(wait_limit=1000, extra_dependency=1)  # about 0.1 ms per wait
+    plan(d, ws)
+    torch.cuda.synchronize()
+    assert plan.status() == 1
+    # the short item has no dependency and is still transformed
+    off, n, c = items[1]
+    ref = np.fft.fft(x[off: off + n * c].reshape(c, n).astype(np.complex128), axis=-1)
+    assert rel_l2(d.cpu().numpy()[off: off + n * c].reshape(c, n), ref) <= 2 * tol_fp32(n)
+    # restore: the same plan, then a fresh plan, run clean on the same stream
+    plan.set_wait()
+    assert plan.status() == 0
+    d.copy_(torch.from_numpy(x))
+    plan(d, ws)
+    other = BatchPlan(pack_items([(65536, 1)])[0])
+    y = torch.from_numpy((rng.standard_normal(65536) + 1j * rng.standard_normal(65536)).astype(np.complex64)).cuda()
+    y0 = y.cpu().numpy()
+    other(y, other.make_workspace())
+    torch.cuda.synchronize()
+    assert plan.status() == 0 and other.status() == 0
+    got = d.cpu().numpy()
+    for off, n, c in items:
+        ref = np.fft.fft(x[off: off + n * c].reshape(c, n).astype(np.complex128), axis=-1)
+        assert rel_l2(got[off: off + n * c].reshape(c, n), ref) <= 2 * tol_fp32(n)
+    assert rel_l2(y.cpu().numpy(), np.fft.fft(y0.astype(np.complex128))) <= 2 * tol_fp32(65536)
+
+
+def test_set_wait_validation():
+    plan = BatchPlan([(0, 64, 1)])
+    with pytest.raises(ValueError):
+        plan.set_wait(wait_limit=0)
+    with pytest.raises(ValueError):
+        plan.set_wait(extra_dependency=-1)

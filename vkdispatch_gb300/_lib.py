@@ -57,6 +57,7 @@ EXPORTED = (
     "vdx_batch_workspace_bytes",
     "vdx_batch_exec",
     "vdx_batch_status",
+    "vdx_batch_plan_set_wait",
 )
 VDX_REDUCE_NOALLOC_SCRATCH_BYTES = 1048576
 
@@ -153,6 +154,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.vdx_batch_exec.argtypes = [vp, vp, vp, vp]
     lib.vdx_batch_status.restype = i32
     lib.vdx_batch_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+    lib.vdx_batch_plan_set_wait.restype = i32
+    lib.vdx_batch_plan_set_wait.argtypes = [vp, i64, i32]
     lib.vdx_reduce_noalloc.restype = i32
     lib.vdx_reduce_noalloc.argtypes = [i32, i32, i32, vp, i64, i64, vp, vp]
 

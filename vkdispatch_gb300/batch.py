@@ -97,6 +97,13 @@ class BatchPlan:
         G.resolve(graph).record(lambda s: L.check(L.lib().vdx_batch_exec(h, dptr, wptr, s), "batch exec"),
                                 (data, workspace))
 
+    def set_wait(self, wait_limit: int = 1 << 22, extra_dependency: int = 0) -> None:
+        """Poll limit of the launch's dependency waits, and an optional
+        injected unmet dependency (see vdx_batch_plan_set_wait); clears the
+        status word.  Synchronous."""
+        L.check(L.lib().vdx_batch_plan_set_wait(self.handle, int(wait_limit), int(extra_dependency)),
+                "batch set_wait")
+
     def status(self) -> int:
         """0, or 1 when a dependency wait inside a launch gave up (synchronous)."""
         st = ctypes.c_int()

@@ -35,7 +35,7 @@ namespace vdx {
 namespace {
 
 constexpr int kMaxBatchThreads = 1024;
-constexpr long long kWaitLimit = 1ll << 22;  // polls of ~100 ns before a dependency wait gives up
+constexpr long long kWaitLimit = 1ll << 22;  // default polls of ~100 ns before a dependency wait gives up
 
 enum UnitKind { UK_ROWS = 0, UK_COLS = 1, UK_ROWS2 = 2 };
 
@@ -70,6 +70,8 @@ struct BatchArgs {
   unsigned* ticket;
   int* counters;
   int* status;
+  long long wait_limit;  // polls before a dependency wait gives up
+  int extra_wait;        // added to every dependency count (0 unless a test injects an unmet dependency)
 };
 
 // placement of a thread inside the current unit (the interface run_passes
@@ -198,9 +200,9 @@ __global__ void __launch_bounds__(THREADS, MINB) k_batch(BatchArgs a) {
       if (tid == 0) {
         int ok = 1;
         long long polls = 0;
-        const int item = wu.item, wait = wu.wait;
+        const int item = wu.item, wait = wu.wait + a.extra_wait;
         while (atomicAdd(&a.counters[item], 0) < wait) {
-          if (++polls > kWaitLimit) {
+          if (++polls > a.wait_limit) {
             atomicExch(a.status, 1);
             ok = 0;
             break;
@@ -266,6 +268,8 @@ struct vdx_batch_plan {
   unsigned* d_ticket;
   int* d_counters;
   int* d_status;
+  long long wait_limit = vdx::kWaitLimit;
+  int extra_wait = 0;
   std::string desc;
 };
 
@@ -547,6 +551,8 @@ int vdx_batch_exec(const vdx_batch_plan* p, void* data, void* workspace, void* s
   a.ticket = p->d_ticket;
   a.counters = p->d_counters;
   a.status = p->d_status;
+  a.wait_limit = p->wait_limit;
+  a.extra_wait = p->extra_wait;
   Launch l;
   l.grid = dim3(p->grid);
   l.block = dim3(p->cta);
@@ -558,6 +564,17 @@ int vdx_batch_exec(const vdx_batch_plan* p, void* data, void* workspace, void* s
     default: e = p->inverse ? enqueue(k_batch<true, 1024, 1>, l, a) : enqueue(k_batch<false, 1024, 1>, l, a); break;
   }
   if (e != cudaSuccess) return set_error(VDX_ERR_CUDA, cudaGetErrorString(e));
+  return VDX_OK;
+}
+
+int vdx_batch_plan_set_wait(vdx_batch_plan* p, int64_t wait_limit, int32_t extra_dependency) {
+  if (!p) return set_error(VDX_ERR_INVALID, "plan must be non-NULL");
+  if (wait_limit < 1 || extra_dependency < 0)
+    return set_error(VDX_ERR_INVALID, "wait_limit must be >= 1 and extra_dependency >= 0");
+  cudaError_t e = cudaMemset(p->d_status, 0, sizeof(int));
+  if (e != cudaSuccess) return set_error(VDX_ERR_CUDA, cudaGetErrorString(e));
+  p->wait_limit = wait_limit;
+  p->extra_wait = extra_dependency;
   return VDX_OK;
 }
 
