@@ -316,6 +316,11 @@ def _run_ours(args):
     if rank == 0 and not args.quick:
         extra["rfft2_irfft2_roundtrip_64x512x512"] = roundtrip_numbers(vd, torch, flush, images)
     if rank == 0 and not args.quick:
+        try:
+            extra["reference_kernels_gb300"] = reference_kernels_numbers(torch, flush, images, kernel, kspec.tensor)
+        except Exception as exc:  # report, do not fail the benchmark
+            extra["reference_kernels_gb300"] = {"error": str(exc)[:300]}
+        torch.cuda.empty_cache()
         extra["diff_conv3d_256"] = diff_conv3d_numbers(torch, flush)
         extra["batched_uneven_4096_lengths_2p28"] = batched_uneven_numbers(torch)
         extra["mixed_precision_fft2_16384"] = mixed_precision_numbers(torch)
@@ -390,6 +395,213 @@ def compact(obj, drop=("plans", "plan")):
     if isinstance(obj, float) and math.isfinite(obj) and obj != 0.0:
         return float(f"{obj:.4g}")
     return obj
+
+
+class ReferenceKernels:
+    """The reference's own generated CUDA kernels for these workloads
+    (baseline/make_reference_kernels.py writes and compiles them into
+    baseline/_ref_kernels/), launched with the reference's grid and block
+    shapes: a GPU comparator, never part of the measured arm."""
+
+    DIR = ROOT / "baseline" / "_ref_kernels"
+
+    def __init__(self):
+        import ctypes
+
+        self.ctypes = ctypes
+        self.table = json.loads((self.DIR / "kernels.json").read_text())
+        self.built = json.loads((self.DIR / "built.json").read_text())
+        self.libs = {}
+
+    @classmethod
+    def available(cls):
+        return (cls.DIR / "built.json").exists()
+
+    def why_not(self, name):
+        t = self.table.get(name, {})
+        return t.get("unavailable") or self.built.get(name)
+
+    def launch(self, name, ptrs, stream):
+        ct = self.ctypes
+        if name not in self.libs:
+            lib = ct.CDLL(str(self.DIR / f"{name}.so"))
+            lib.vdref_launch.restype = ct.c_int
+            lib.vdref_launch.argtypes = [ct.POINTER(ct.c_void_p), ct.c_char_p] + [ct.c_uint] * 6 + [ct.c_void_p]
+            self.libs[name] = lib
+        t = self.table[name]
+        arr = (ct.c_void_p * len(ptrs))(*ptrs)
+        ubo = bytes(t["ubo"]) if t["ubo"] else b"\0" * 64
+        rc = self.libs[name].vdref_launch(arr, ubo, *t["grid"], *t["local"], stream)
+        if rc != 0:
+            raise RuntimeError(f"reference kernel {name}: CUDA error {rc}")
+
+
+def _slack(torch, shape, dtype):
+    """A device tensor of `shape` inside an allocation with 1 MiB of slack
+    after it."""
+    n = int(np.prod(shape))
+    esz = torch.empty((), dtype=dtype).element_size()
+    raw = torch.zeros(n + (1 << 20) // esz, dtype=dtype, device="cuda")
+    return raw[:n].view(shape), raw
+
+
+def reference_kernels_numbers(torch, flush, images, kernel, kspec_tensor, reps=20):
+    """The reference's generated kernels on this GPU, on the same inputs as
+    the measured arm: the convolve2DR step (rfft rows -> conv axis 1 -> irfft
+    rows), the 1024-point C2C pair with its magnitude sum, the HBM-scale C2C,
+    and the 256^3 convolution forward schedule; GB/s by the same algorithmic
+    bytes, errors against FP64."""
+    if not ReferenceKernels.available():
+        return {"unavailable": "reference kernels not generated here (baseline/make_reference_kernels.py)"}
+    rk = ReferenceKernels()
+    st = lambda: int(torch.cuda.current_stream().cuda_stream)  # noqa: E731
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    peak, _ = _load_peaks()
+    out = {}
+
+    def timed(fn, n=reps, flush_l2=True):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(n):
+            if flush_l2:
+                flush.zero_()
+            ev[0].record()
+            fn()
+            ev[1].record()
+            torch.cuda.synchronize()
+            ts.append(ev[0].elapsed_time(ev[1]))
+        return statistics.median(ts)
+
+    # convolve2DR on 64 x 512 x 512
+    names = ("cfg2_rfft", "cfg2_conv", "cfg2_irfft")
+    bad = [f"{n}: {rk.why_not(n)}" for n in names if rk.why_not(n)]
+    if bad:
+        out["convolve2DR_64x512x512"] = {"unavailable": "; ".join(bad)}
+    else:
+        rows, raw = _slack(torch, (B, H, 2 * HC), torch.float32)
+        h_in = torch.zeros((B, H, 2 * HC), dtype=torch.float32)
+        h_in[..., :W] = torch.from_numpy(images)
+        d_in = h_in.cuda()
+        p = rows.data_ptr()
+        kp = kspec_tensor.data_ptr()
+
+        def step():
+            rk.launch("cfg2_rfft", [p], st())
+            rk.launch("cfg2_conv", [p, kp], st())
+            rk.launch("cfg2_irfft", [p], st())
+
+        rows.copy_(d_in)
+        step()
+        torch.cuda.synchronize()
+        got = rows[..., :W].cpu().numpy()
+        ref = reference_fp64(images, kernel)
+        err = float(np.linalg.norm((got - ref).ravel()) / np.linalg.norm(ref.ravel()))
+        step_ms = timed(step)  # a normalised smoothing kernel: repeated steps stay in range
+        per = {}
+        for n in names:
+            ptrs = [p, kp] if n == "cfg2_conv" else [p]
+            per[n] = round(timed(lambda n=n, ptrs=ptrs: rk.launch(n, ptrs, st())), 4)
+        out["convolve2DR_64x512x512"] = {
+            "ms_per_step": round(step_ms, 4), "GBps": round(STEP_BYTES / (step_ms * 1e-3) / 1e9, 1),
+            "frac_of_measured_hbm": round(STEP_BYTES / (step_ms * 1e-3) / 1e9 / peak, 4),
+            "per_kernel_ms": per, "error_rel_l2_vs_fp64": err,
+            "launch": {n: [rk.table[n]["grid"][0], rk.table[n]["local"]] for n in names}}
+        del rows, raw, d_in
+
+    # 256 x 1024 C2C fwd + inv + magnitude sum, and the HBM-scale C2C
+    rng = np.random.default_rng(0)
+    x = (rng.standard_normal((256, 1024)) + 1j * rng.standard_normal((256, 1024))).astype(np.complex64)
+    names = ("cfg1_fft", "cfg1_ifft", "cfg1_magsum_s1", "cfg1_magsum_s2")
+    bad = [f"{n}: {rk.why_not(n)}" for n in names if rk.why_not(n)]
+    if bad:
+        out["c2c_256x1024_fwd_inv_magsum"] = {"unavailable": "; ".join(bad)}
+    else:
+        b, rawb = _slack(torch, (256, 1024), torch.complex64)
+        b.copy_(torch.from_numpy(x))
+        red, rawr = _slack(torch, (257,), torch.float32)
+
+        def small():
+            rk.launch("cfg1_fft", [b.data_ptr()], st())
+            rk.launch("cfg1_ifft", [b.data_ptr()], st())
+            rk.launch("cfg1_magsum_s1", [red.data_ptr(), b.data_ptr()], st())
+            rk.launch("cfg1_magsum_s2", [red.data_ptr()], st())
+
+        small()
+        torch.cuda.synchronize()
+        ref_sum = float(np.abs(x.astype(np.complex128)).sum())
+        ms = timed(small, n=200, flush_l2=False)
+        out["c2c_256x1024_fwd_inv_magsum"] = {
+            "ms_per_step": round(ms, 5), "GBps": round(10485760 / (ms * 1e-3) / 1e9, 1),
+            "magnitude_sum": float(red[0].item()), "magnitude_sum_rel_err_vs_fp64": abs(red[0].item() - ref_sum) / ref_sum}
+        del b, rawb, red, rawr
+    res = {}
+    for nm in ("cfg1_hbm_fft", "cfg1_hbm_ifft"):
+        if rk.why_not(nm):
+            res[nm] = {"unavailable": rk.why_not(nm)}
+            continue
+        big, rawbig = _slack(torch, (262144, 1024), torch.complex64)
+        big.normal_()
+        ms = timed(lambda: rk.launch(nm, [big.data_ptr()], st()), n=10)
+        gbps = 2 * big.numel() * 8 / (ms * 1e-3) / 1e9
+        res["fwd" if nm.endswith("_fft") else "inv"] = {"ms": round(ms, 4), "GBps": round(gbps, 1),
+                                                         "frac_of_measured_hbm": round(gbps / peak, 4)}
+        del big, rawbig
+        torch.cuda.empty_cache()
+    out["c2c_hbm_1024x262144"] = res
+
+    # the 256^3 convolution's forward schedule (fft ax0, fft ax1, conv ax2,
+    # ifft ax1, ifft ax0), against the same schedule on libvdx's plain kernels
+    names = ("cfg3_fft_ax0", "cfg3_fft_ax1", "cfg3_conv_ax2", "cfg3_ifft_ax1", "cfg3_ifft_ax0")
+    bad = [f"{n}: {rk.why_not(n)}" for n in names if rk.why_not(n)]
+    if bad:
+        out["conv3d_256_forward"] = {"unavailable": "; ".join(bad)}
+    else:
+        import vkdispatch_gb300 as vd
+
+        n3 = 256
+        g = torch.Generator(device="cuda").manual_seed(2)
+        x3 = torch.randn((n3, n3, n3), dtype=torch.complex64, device="cuda", generator=g)
+        k3 = 0.1 * torch.randn((n3, n3, n3), dtype=torch.complex64, device="cuda", generator=g)
+        a3, rawa = _slack(torch, (n3, n3, n3), torch.complex64)
+
+        def ref_fwd():
+            pa = a3.data_ptr()
+            for nm in names:
+                rk.launch(nm, [pa, k3.data_ptr()] if "conv" in nm else [pa], st())
+
+        ours = vd.from_cuda_array(a3)
+        kb = vd.from_cuda_array(k3)
+
+        def our_fwd():
+            vd.fft.fft(ours, axis=0)
+            vd.fft.fft(ours, axis=1)
+            vd.fft.convolve(ours, kb, axis=2)
+            vd.fft.ifft(ours, axis=1)
+            vd.fft.ifft(ours, axis=0)
+
+        want = torch.fft.ifftn(torch.fft.fftn(x3.to(torch.complex128)) * k3.to(torch.complex128).conj())
+        errs = {}
+        for nm, fn in (("reference", ref_fwd), ("libvdx", our_fwd)):
+            a3.copy_(x3)
+            fn()
+            torch.cuda.synchronize()
+            errs[nm] = float(torch.linalg.vector_norm(a3.to(torch.complex128) - want) / torch.linalg.vector_norm(want))
+        del want
+        alg = 5 * 268435456 + 134217728
+        t_ref = timed(lambda: (a3.copy_(x3), ref_fwd()) and None) - timed(lambda: a3.copy_(x3))
+        t_ours = timed(lambda: (a3.copy_(x3), our_fwd()) and None) - timed(lambda: a3.copy_(x3))
+        out["conv3d_256_forward"] = {
+            "reference_ms": round(t_ref, 4), "libvdx_ms": round(t_ours, 4),
+            "reference_GBps": round(alg / (t_ref * 1e-3) / 1e9, 1), "libvdx_GBps": round(alg / (t_ours * 1e-3) / 1e9, 1),
+            "speedup": round(t_ref / t_ours, 3), "reference_rel_l2_vs_fp64": errs["reference"],
+            "libvdx_rel_l2_vs_fp64": errs["libvdx"]}
+        del x3, k3, a3, rawa
+    for nm in ("cfg5_fft_ax0", "cfg5_fft_ax1"):
+        if rk.why_not(nm):
+            out.setdefault("fft2_16384_c64", {})[nm] = "reference N/A: " + str(rk.why_not(nm))
+    torch.cuda.empty_cache()
+    return out
 
 
 def c2c1024_numbers(vd, torch, flush, args):

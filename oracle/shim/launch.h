@@ -1,6 +1,8 @@
 // Launch loop for a generated kernel compiled against cuda_runtime.h above.
 #pragma once
 
+#include <algorithm>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -10,6 +12,8 @@ uint3 bid;
 dim3 bdim;
 dim3 gdim;
 std::barrier<>* bar;
+thread_local int lin;
+Warp* warps;
 
 template <class F>
 void run_grid(dim3 grid, dim3 block, F&& body) {
@@ -22,11 +26,20 @@ void run_grid(dim3 grid, dim3 block, F&& body) {
         bid = uint3{bx, by, bz};
         std::barrier<> b(nthreads);
         bar = &b;
+        const int nwarps = (nthreads + 31) / 32;
+        std::vector<Warp> ws(nwarps);
+        std::vector<std::unique_ptr<std::barrier<>>> wbars;
+        for (int w = 0; w < nwarps; ++w) {
+          wbars.emplace_back(new std::barrier<>(std::min(32, nthreads - 32 * w)));
+          ws[w].bar = wbars.back().get();
+        }
+        warps = ws.data();
         std::vector<std::thread> ts;
         ts.reserve(nthreads);
         for (int t = 0; t < nthreads; ++t)
           ts.emplace_back([&, t] {
             tid = uint3{unsigned(t % block.x), unsigned((t / block.x) % block.y), unsigned(t / (block.x * block.y))};
+            lin = t;
             body();
           });
         for (auto& th : ts) th.join();

@@ -1,10 +1,10 @@
 """Generates the golden fixtures under tests/golden/ by importing the
 reference (sharhar/vkdispatch) from a local checkout.
 
-Run in a container that has the reference checkout (default: the
-VKDISPATCH_REFERENCE environment variable, else /root/reference):
+Run where a reference checkout exists, naming it with the
+VKDISPATCH_REFERENCE environment variable:
 
-    python tests/golden/make_golden.py [plans|vectors|all]
+    VKDISPATCH_REFERENCE=<checkout> python tests/golden/make_golden.py [plans|vectors|config|all]
 
 plans   -> plans.json: the reference's own FFT plan (prime groups per stage,
            register count, threads per transform) for every 13-smooth length
@@ -13,8 +13,14 @@ plans   -> plans.json: the reference's own FFT plan (prime groups per stage,
            48 KiB shared memory, 32-wide subgroups).
 vectors -> vectors.npz: inputs and outputs of the reference's own generated
            FFT / convolution / R2C / C2R kernels, emitted by its CUDA code
-           generator and executed on the host through oracle/cuda_host_shim.h
+           generator and executed on the host through oracle/shim/
            (see oracle/run_reference_kernels.py).
+config  -> config_vectors.npz: the same at the benchmark configurations'
+           lengths and stride classes (1024-point rows forward and inverse,
+           512-point R2C / C2R rows, the 512 x 257 strided convolution, a
+           32^3 FFT3) plus the reference's two-stage reductions (magnitude
+           sum, uint32 xor, int32 and, float sum); inputs come from
+           oracle/inputs.py and large outputs are kept at sampled indices.
 
 Only the fixtures are committed; the reference and its generated sources are
 not.  Nothing at test time reads the reference.
@@ -28,7 +34,7 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF = os.environ.get("VKDISPATCH_REFERENCE", "/root/reference")
+REF = os.environ.get("VKDISPATCH_REFERENCE")
 
 GB300_LIMITS = dict(
     subgroup_size=32,
@@ -87,6 +93,8 @@ def make_plans():
 
 
 if __name__ == "__main__":
+    if not REF:
+        sys.exit("set VKDISPATCH_REFERENCE to the reference checkout")
     what = sys.argv[1] if len(sys.argv) > 1 else "all"
     if what in ("plans", "all"):
         make_plans()
@@ -95,3 +103,8 @@ if __name__ == "__main__":
         from oracle import run_reference_kernels
 
         run_reference_kernels.make_vectors(REF, HERE / "vectors.npz", GB300_LIMITS)
+    if what in ("config", "all"):
+        sys.path.insert(0, str(HERE.parent.parent))
+        from oracle import run_reference_kernels
+
+        run_reference_kernels.make_config_vectors(REF, HERE / "config_vectors.npz", GB300_LIMITS)

@@ -1,6 +1,6 @@
 """GPU parity against the golden vectors: outputs of the reference's own
 generated kernels (tests/golden/vectors.npz), compared with libvdx through
-the vd-compatible API within the fp32 tolerance."""
+the vd-compatible API within the plain fp32 bound."""
 
 import json
 from pathlib import Path
@@ -45,4 +45,7 @@ def test_matches_reference_kernel_outputs(name):
         b, k = vd.asbuffer(x), vd.asbuffer(G[name + "__kernel"])
         vd.fft.convolve(b, k, axis=ax)
         got = b.read(0)
-    assert rel_l2(got, want) <= 2 * tol_fp32(n), name
+    # the benchmark spec's plain bound: 5e-7 log2 N per pass (a convolution is
+    # two passes); the reference's own outputs sit at about 3% of it
+    passes = 2 if kind == "conv" else 1
+    assert rel_l2(got, want) <= tol_fp32(*([n] * passes)), name

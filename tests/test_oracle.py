@@ -124,3 +124,69 @@ def test_reduce_restatement():
     assert ref.reduce_f32(d, op="min")[0] == d.min()
     c = (rng.standard_normal(5000) + 1j * rng.standard_normal(5000)).astype(np.complex64)
     assert abs(ref.reduce_f32(c, map="abs")[0] - np.abs(c.astype(np.complex128)).sum()) < 1e-3
+
+
+# ---------------------------------------------------------------------------
+# config-shape fixtures (tests/golden/config_vectors.npz): inputs regenerated
+# from oracle/inputs.py, outputs of the reference's own generated kernels
+# (sampled where large)
+# ---------------------------------------------------------------------------
+from oracle import inputs  # noqa: E402
+
+CG = np.load(GOLDEN / "config_vectors.npz")
+CMETA = json.loads(bytes(CG["__meta__"]).decode())
+
+
+def _at(name, arr):
+    flat = np.ascontiguousarray(arr).reshape(-1)
+    return flat if CMETA[name]["full"] else flat[CG[name + "__idx"]]
+
+
+def _cfg1_chain():
+    x = inputs.complex_uniform(101, (256, 1024))
+    y = ref.fft(x, axis=1)
+    return y, ref.fft(y, axis=1, inverse=True)
+
+
+def test_config_cfg1_forward_inverse_bit_exact():
+    y, z = _cfg1_chain()
+    assert np.array_equal(_at("cfg1_fwd", y), CG["cfg1_fwd"])
+    assert np.array_equal(_at("cfg1_inv", z), CG["cfg1_inv"])
+
+
+def test_config_cfg1_magnitude_sum_bit_exact():
+    """The reference's two-stage map_reduce (sqrt(re^2 + im^2), add) over the
+    inverse output: the restatement's fold order gives its exact bits."""
+    _, z = _cfg1_chain()
+    got = ref.reduce_f32(z.reshape(-1), "add", "abs")
+    assert got[0] == CG["cfg1_magsum"][0]
+
+
+def test_config_512_point_real_rows_bit_exact():
+    xr = inputs.uniform(102, (8, 512))
+    assert np.array_equal(_at("r2c_8x512", ref.rfft_packed(ref.packed_from_real(xr), 512)), CG["r2c_8x512"])
+    spec = inputs.complex_uniform(103, (8, 257))
+    got = ref.real_from_packed(ref.irfft_packed(spec, 512), 512)
+    assert np.array_equal(_at("c2r_8x512", got), CG["c2r_8x512"])
+
+
+def test_config_strided_conv_512x257_bit_exact():
+    xs = inputs.complex_uniform(104, (2, 512, 257))
+    ks = inputs.complex_uniform(105, (2, 512, 257))
+    assert np.array_equal(_at("conv_2x512x257_ax1", ref.convolve(xs, ks, axis=1)), CG["conv_2x512x257_ax1"])
+
+
+def test_config_fft3_32_bit_exact():
+    b = inputs.complex_uniform(106, (32, 32, 32))
+    for ax in (0, 1, 2):
+        b = ref.fft(b, axis=ax)
+    assert np.array_equal(_at("fft3_32", b), CG["fft3_32"])
+
+
+def test_config_reductions():
+    u = inputs.uint32(107, (3, 100003))
+    assert np.array_equal(CG["xor_u32_3x100003"][:3], np.bitwise_xor.reduce(u, axis=1))
+    i = inputs.uint32(109, (3 * 100003,)).view(np.int32) | np.int32(0x10204081)
+    assert np.array_equal(CG["and_i32_3x100003"][:3], np.bitwise_and.reduce(i.reshape(3, -1), axis=1))
+    f = inputs.uniform(108, (3 * 300001,))
+    assert np.array_equal(ref.reduce_f32(f, "add", "identity", batch=3), CG["sum_f32_3x300001"][:3])
