@@ -339,6 +339,51 @@ int vdx_reduce(int op, int map, int in_type, const void* in, int64_t n, int64_t 
 int vdx_reduce_noalloc(int op, int map, int in_type, const void* in, int64_t n, int64_t batch, void* out,
                        void* stream);
 
+/*
+ * Map hooks compiled at run time.  The reference injects arbitrary user code
+ * at the FFT's loads, stores and spectrum multiply: input_map / output_map /
+ * kernel_map callbacks traced into its generated shader
+ * (vkdispatch/fft/io_manager.py:107-155, vkdispatch/shader/map.py:29-40,
+ * compiled by vkdispatch/backends/cuda_backend/api_compute.py:30-70).  Here
+ * the caller supplies those callbacks as a C++ source fragment defining
+ *
+ *   struct VdxHooks {
+ *     template <class Re> __device__ static vdx::Cx<Re> load(const vdx::MapArgs& m, long long io, int k, int n);
+ *     template <class Re> __device__ static void store(const vdx::MapArgs& m, vdx::Cx<Re> v, long long io,
+ *                                                      int k, int n);
+ *     template <class Re> __device__ static vdx::Cx<Re> kernel(const vdx::MapArgs& m, vdx::Cx<Re> v,
+ *                                                               long long io, int k, int n);
+ *   };
+ *
+ * (io = the element's flat index in the descriptor's shape, the reference's
+ * io_index; k = fft_index; n = fft_size; m = the vdx_map_args of the call),
+ * and libvdx compiles it with NVRTC into its own Stockham kernel template
+ * (csrc/fft_mapped.cuh), specialised to the plan's compile-time radix list.
+ * The descriptor is a C2C (load, passes, store) or CONV (load, forward,
+ * kernel, inverse, store) descriptor of complex64 or complex128 compute with
+ * io_type equal to compute_type; axes that need a four-step or Bluestein
+ * plan are refused.  Compilation happens at plan creation (about a second;
+ * cached per source, plan shape and device) and needs NVRTC and the CUDA
+ * headers at run time (VDX_CUDA_INCLUDE or CUDA_HOME name them when they are
+ * not in the default locations); its log is returned through
+ * vdx_last_error on failure.  vdx_map_exec is one asynchronous launch.
+ */
+#define VDX_MAP_MAX_BUFFERS 8
+#define VDX_MAP_MAX_SCALARS 8
+typedef struct vdx_map_args {
+  void* buffers[VDX_MAP_MAX_BUFFERS];  /* device pointers the hooks index */
+  double fscalars[VDX_MAP_MAX_SCALARS]; /* floating-point map arguments */
+  int64_t iscalars[VDX_MAP_MAX_SCALARS]; /* integer map arguments */
+  int64_t kernel_index;                /* mapped_kernel_index() of a multi-kernel convolution */
+} vdx_map_args;
+
+typedef struct vdx_map_plan vdx_map_plan;
+int vdx_map_plan_create(const vdx_fft_desc* desc, const char* hooks_source, vdx_map_plan** plan);
+int vdx_map_plan_destroy(vdx_map_plan* plan);
+int vdx_map_exec(const vdx_map_plan* plan, const vdx_map_args* args, void* stream);
+/* The full source NVRTC compiled for the plan (hooks and instantiation). */
+int vdx_map_plan_source(const vdx_map_plan* plan, char* buf, size_t n);
+
 #ifdef __cplusplus
 }
 #endif

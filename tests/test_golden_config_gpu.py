@@ -86,7 +86,7 @@ def test_integer_reductions_bit_exact():
     def xor_u(a: u32, b: u32) -> u32:
         return a ^ b
 
-    assert np.array_equal(xor_u(u).read(0)[:3].astype(np.uint32), G["xor_u32_3x100003"][:3])
+    assert np.array_equal(xor_u(u).read(0).reshape(-1)[:3].astype(np.uint32), G["xor_u32_3x100003"][:3])
     i = inputs.uint32(109, (3 * 100003,)).view(np.int32) | np.int32(0x10204081)
     ib = vd.asbuffer(i.reshape(3, 100003))
 
@@ -94,7 +94,7 @@ def test_integer_reductions_bit_exact():
     def and_i(a: i32, b: i32) -> i32:
         return a & b
 
-    assert np.array_equal(and_i(ib).read(0)[:3].astype(np.int32), G["and_i32_3x100003"][:3])
+    assert np.array_equal(and_i(ib).read(0).reshape(-1)[:3].astype(np.int32), G["and_i32_3x100003"][:3])
 
 
 def test_float_sum_rows():
@@ -105,7 +105,7 @@ def test_float_sum_rows():
     def sum_f(a: f32, b: f32) -> f32:
         return a + b
 
-    got = sum_f(fb).read(0)[:3].astype(np.float64)
+    got = sum_f(fb).read(0).reshape(-1)[:3].astype(np.float64)
     want = G["sum_f32_3x300001"][:3].astype(np.float64)
     bound = 2 * np.finfo(np.float32).eps * np.log2(300001) * np.abs(f.astype(np.float64)).sum(axis=1)
     assert np.all(np.abs(got - want) <= bound)

@@ -2,7 +2,9 @@
 
 Translation units compile in parallel into ``_build/`` and link into
 ``vkdispatch_gb300/libvdx.so`` (both git-ignored).  Objects are rebuilt when
-their source or any header is newer.
+their source or any header is newer.  The kernel headers that the run-time
+compiled map kernels include (JIT_HEADERS) are embedded into
+``_build/jit_headers.inc`` as string literals for jit.cu.
 """
 
 from __future__ import annotations
@@ -30,7 +32,11 @@ NVCC_FLAGS = [
     "-fPIC",
     f"-I{INCLUDE}",
     f"-I{CSRC}",
+    f"-I{BUILD_DIR}",
 ]
+
+# headers NVRTC compiles the map kernels from (csrc/jit.cu), in include order
+JIT_HEADERS = ("vdx_common.cuh", "fft_kernels.cuh", "fft_mapped.cuh")
 
 
 def nvcc_path() -> str:
@@ -54,9 +60,29 @@ def _compile(nvcc: str, src: Path, obj: Path, verbose: bool) -> None:
         raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stdout}\n{r.stderr}")
 
 
+def _write_jit_headers() -> None:
+    """_build/jit_headers.inc: the JIT_HEADERS as C++ raw string literals
+    (rewritten only when their text changes)."""
+    names, bodies = [], []
+    for h in JIT_HEADERS:
+        text = (CSRC / h).read_text()
+        delim = "VDXJIT"
+        assert f"){delim}\"" not in text
+        names.append(f'"{h}"')
+        bodies.append(f'R"{delim}({text}){delim}"')
+    inc = ("// generated by vkdispatch_gb300/_build.py from csrc/" + ", ".join(JIT_HEADERS) + "\n"
+           f"static const int kJitHeaderCount = {len(JIT_HEADERS)};\n"
+           "static const char* const kJitHeaderNames[] = {" + ", ".join(names) + "};\n"
+           "static const char* const kJitHeaderSources[] = {\n" + ",\n".join(bodies) + "};\n")
+    out = BUILD_DIR / "jit_headers.inc"
+    if not out.exists() or out.read_text() != inc:
+        out.write_text(inc)
+
+
 def build(verbose: bool = False, force: bool = False) -> Path:
     nvcc = nvcc_path()
     BUILD_DIR.mkdir(exist_ok=True)
+    _write_jit_headers()
     srcs = sorted(CSRC.glob("*.cu"))
     hdr = _headers_mtime()
     jobs = []
@@ -75,7 +101,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     newest = max(o.stat().st_mtime for o in objs)
     if force or jobs or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < newest:
         tmp = LIB_PATH.with_suffix(".so.tmp")
-        cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", str(tmp), *map(str, objs)]
+        cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", str(tmp), *map(str, objs), "-ldl"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

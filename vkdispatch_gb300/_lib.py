@@ -58,6 +58,10 @@ EXPORTED = (
     "vdx_batch_exec",
     "vdx_batch_status",
     "vdx_batch_plan_set_wait",
+    "vdx_map_plan_create",
+    "vdx_map_plan_destroy",
+    "vdx_map_exec",
+    "vdx_map_plan_source",
 )
 VDX_REDUCE_NOALLOC_SCRATCH_BYTES = 1048576
 
@@ -91,6 +95,17 @@ class ExecOps(ctypes.Structure):
         ("spec_aux", ctypes.c_void_p),
         ("loss_weight", ctypes.c_void_p),
         ("loss_partials", ctypes.c_void_p),
+    ]
+
+
+class MapArgs(ctypes.Structure):
+    """vdx_map_args: the buffers and scalars a run-time compiled map reads."""
+
+    _fields_ = [
+        ("buffers", ctypes.c_void_p * 8),
+        ("fscalars", ctypes.c_double * 8),
+        ("iscalars", ctypes.c_int64 * 8),
+        ("kernel_index", ctypes.c_int64),
     ]
 
 
@@ -156,6 +171,14 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.vdx_batch_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     lib.vdx_batch_plan_set_wait.restype = i32
     lib.vdx_batch_plan_set_wait.argtypes = [vp, i64, i32]
+    lib.vdx_map_plan_create.restype = i32
+    lib.vdx_map_plan_create.argtypes = [ctypes.POINTER(FftDesc), ctypes.c_char_p, ctypes.POINTER(vp)]
+    lib.vdx_map_plan_destroy.restype = i32
+    lib.vdx_map_plan_destroy.argtypes = [vp]
+    lib.vdx_map_exec.restype = i32
+    lib.vdx_map_exec.argtypes = [vp, ctypes.POINTER(MapArgs), vp]
+    lib.vdx_map_plan_source.restype = i32
+    lib.vdx_map_plan_source.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     lib.vdx_reduce_noalloc.restype = i32
     lib.vdx_reduce_noalloc.argtypes = [i32, i32, i32, vp, i64, i64, vp, vp]
 

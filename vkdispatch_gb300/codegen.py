@@ -57,6 +57,30 @@ class Sym:
 
     __rmul__ = __mul__
 
+    def __rsub__(self, o):
+        return Sym("sub", o, self)
+
+    def __truediv__(self, o):
+        return self._bin("div", o)
+
+    def __rtruediv__(self, o):
+        return Sym("div", o, self)
+
+    def __floordiv__(self, o):
+        return self._bin("floordiv", o)
+
+    def __rfloordiv__(self, o):
+        return Sym("floordiv", o, self)
+
+    def __mod__(self, o):
+        return self._bin("mod", o)
+
+    def __rmod__(self, o):
+        return Sym("mod", o, self)
+
+    def to_register(self, var_name=None):
+        return self
+
     def __and__(self, o):
         return self._bin("and", o)
 
@@ -104,7 +128,34 @@ class SymBuffer:
         self.var_type = var_type
 
     def __getitem__(self, idx):
-        return Sym("load", self.index)
+        return Sym("load", self.index, idx)
+
+
+class SymVec(tuple):
+    """Integer vector of index components (ravel_index's result)."""
+
+    def to_register(self, var_name=None):
+        return self
+
+
+class _VarType:
+    """Annotation of a scalar map argument (``vc.Var[vc.f32]``)."""
+
+    def __init__(self, t):
+        self.var_type = t
+        self.__args__ = (t,)
+        self.is_scalar = True
+
+    def __repr__(self):
+        return f"Var[{self.var_type.name}]"
+
+
+class _VarFactory:
+    def __getitem__(self, t):
+        return _VarType(t)
+
+
+Var = _VarFactory()
 
 
 class _IoIndex:
@@ -128,6 +179,77 @@ def sqrt(x):
     return Sym("sqrt", x)
 
 
+def _unary(name):
+    def f(x):
+        return Sym(name, x)
+
+    f.__name__ = name
+    return f
+
+
+tan, asin, acos, atan, sinh, cosh, tanh = (_unary(n) for n in ("tan", "asin", "acos", "atan", "sinh", "cosh", "tanh"))
+exp, exp2, log, log2, inversesqrt = (_unary(n) for n in ("exp", "exp2", "log", "log2", "inversesqrt"))
+floor, ceil, trunc, fract, sign = (_unary(n) for n in ("floor", "ceil", "trunc", "fract", "sign"))
+round = _unary("round")  # noqa: A001 - mirrors vc.round
+
+
+def atan2(y, x):
+    return Sym("atan2", y, x)
+
+
+def pow(x, y):  # noqa: A001 - mirrors vc.pow
+    return Sym("pow", x, y)
+
+
+def mod(x, y):
+    return Sym("mod", x, y)
+
+
+def fma(a, b, c):
+    return Sym("fma", a, b, c)
+
+
+def clamp(x, lo, hi):
+    return Sym("clamp", x, lo, hi)
+
+
+clip = clamp
+
+
+def mix(x, y, a):
+    return Sym("mix", x, y, a)
+
+
+def complex_from_euler_angle(angle):
+    return Sym("make", cos(angle), sin(angle))
+
+
+def ravel_index(index, shape):
+    """Flat index -> (x, y[, z]) components in a 2-D or 3-D shape
+    (vkdispatch/codegen/functions/index_raveling.py:55-77)."""
+    shape = tuple(int(v) for v in shape)
+    if len(shape) == 2:
+        return SymVec((index // shape[1], index % shape[1]))
+    if len(shape) == 3:
+        return SymVec((index // (shape[1] * shape[2]), (index // shape[2]) % shape[1], index % shape[2]))
+    raise ValueError(f"Shape must have 2 or 3 elements, not '{shape}'!")
+
+
+def unravel_index(index, shape):
+    """(x, y[, z]) components -> flat index in a 2-D or 3-D shape
+    (vkdispatch/codegen/functions/index_raveling.py:79-96)."""
+    shape = tuple(int(v) for v in shape)
+    if not isinstance(index, (tuple, list)):
+        return index
+    if len(index) > len(shape):
+        raise ValueError(f"Index ({index}) must have the same number of elements as shape ({shape})!")
+    if len(index) == 2:
+        return index[0] * shape[1] + index[1]
+    if len(index) == 3:
+        return index[0] * (shape[1] * shape[2]) + index[1] * shape[2] + index[2]
+    return index[0]
+
+
 def length(x):
     return Sym("length", x)
 
@@ -148,7 +270,7 @@ def max(a, b):  # noqa: A001
 def to_dtype(var_type, *args):
     """Cast (one argument) or build a value of var_type from components."""
     if len(args) == 1:
-        return Sym("cast", args[0])
+        return Sym("cast", args[0], var_type)
     return Sym("make", *args)
 
 
@@ -163,4 +285,19 @@ def mult_complex(a, b):
 def new_register(var_type, *args, var_name=None):
     from .fft import maps
 
-    return maps.new_trace_register(var_type)
+    return maps.new_trace_register(var_type, *args)
+
+
+def new_complex_register(*args, var_name=None):
+    return new_register(c64, *args)
+
+
+new_complex64_register = new_complex_register
+
+
+def new_float_register(*args, var_name=None):
+    return new_register(f32, *args)
+
+
+def new_int_register(*args, var_name=None):
+    return new_register(i32, *args)

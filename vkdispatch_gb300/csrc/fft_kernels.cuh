@@ -141,9 +141,9 @@ struct Place {
 // slots of its own: its exchanges between passes need only warp
 // synchronisation.  Strided column tiles spread a transform over warps.
 template <class PL>
-struct WarpLocal : std::false_type {};
+struct WarpLocal : FalseT {};
 template <>
-struct WarpLocal<Place<false>> : std::true_type {};
+struct WarpLocal<Place<false>> : TrueT {};
 
 __host__ __device__ constexpr bool warp_sized(int T) { return T >= 1 && T <= 32 && 32 % T == 0; }
 
@@ -159,7 +159,7 @@ __device__ __forceinline__ void xsync(bool warp) {
 }
 
 template <int V>
-using IC = std::integral_constant<int, V>;
+using IC = IntConst<int, V>;
 
 // Runtime radix -> compile-time radix.
 template <class F>
@@ -394,15 +394,15 @@ struct FixPlan {
   // PL: a thread placement (Place<STRIDED> or any type with t and sidx(pp, i))
   template <bool INV, bool REV, class PL, class Re>
   __device__ __forceinline__ void run(Cx<Re>* v, const PL& pl, Cx<Re>* sm, const Cx<Re>* tw) const {
-    using Order = typename std::conditional<REV, typename RRev<L>::type, L>::type;
+    using Order = typename Cond<REV, typename RRev<L>::type, L>::type;
     chain_list<N_, T_, MAXE, INV, Re, PL>(Order{}, v, pp, pl, sm, tw);
   }
 };
 
 template <class P>
-struct IsFixPlan : std::false_type {};
+struct IsFixPlan : FalseT {};
 template <int N_, int T_, class L, int MAXE_>
-struct IsFixPlan<FixPlan<N_, T_, L, MAXE_>> : std::true_type {};
+struct IsFixPlan<FixPlan<N_, T_, L, MAXE_>> : TrueT {};
 
 template <class Re>
 __device__ __forceinline__ Cx<Re>* smem_base() {

@@ -1,0 +1,252 @@
+// Map hooks compiled at run time (vdx_map_*).
+//
+// The reference turns every input_map / output_map / kernel_map into code
+// inside the FFT shader it generates and compiles per call
+// (vkdispatch/fft/io_manager.py:107-155, vkdispatch/backends/cuda_backend/
+// api_compute.py:30-70).  Here the FFT kernel stays hand-written
+// (fft_mapped.cuh on the Stockham passes of fft_kernels.cuh); only the hooks
+// struct is user code.  This file compiles the hooks with that template by
+// NVRTC, specialised to the planner's compile-time radix list, and launches
+// the result.  NVRTC is opened with dlopen so that libvdx itself does not
+// depend on it; the kernel headers are embedded at build time.
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+#include <unistd.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fft_mapped.cuh"
+#include "jit_headers.inc"  // kJitHeaderCount, kJitHeaderNames[], kJitHeaderSources[] (written by the build)
+#include "vdx.h"
+#include "vdx_internal.h"
+
+static_assert(sizeof(vdx_map_args) == sizeof(vdx::MapArgs), "vdx_map_args must mirror vdx::MapArgs");
+static_assert(VDX_MAP_MAX_BUFFERS == vdx::kMapMaxBuffers && VDX_MAP_MAX_SCALARS == vdx::kMapMaxScalars,
+              "map argument limits");
+
+namespace {
+
+using namespace vdx;
+
+// ---------------------------------------------------------------------------
+// NVRTC, resolved at first use
+// ---------------------------------------------------------------------------
+struct Nvrtc {
+  decltype(&nvrtcCreateProgram) create = nullptr;
+  decltype(&nvrtcCompileProgram) compile = nullptr;
+  decltype(&nvrtcGetProgramLogSize) log_size = nullptr;
+  decltype(&nvrtcGetProgramLog) log = nullptr;
+  decltype(&nvrtcGetCUBINSize) cubin_size = nullptr;
+  decltype(&nvrtcGetCUBIN) cubin = nullptr;
+  decltype(&nvrtcDestroyProgram) destroy = nullptr;
+  decltype(&nvrtcGetErrorString) error_string = nullptr;
+  std::string where;  // library path, or why it could not be opened
+  bool ok = false;
+};
+
+std::string env(const char* name) {
+  const char* v = std::getenv(name);
+  return v ? std::string(v) : std::string();
+}
+
+const Nvrtc& nvrtc() {
+  static Nvrtc n;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    std::vector<std::string> cands;
+    if (!env("VDX_NVRTC").empty()) cands.push_back(env("VDX_NVRTC"));
+    cands.push_back("libnvrtc.so.13");
+    cands.push_back("libnvrtc.so");
+    for (const char* root : {"CUDA_HOME", "CUDA_PATH"})
+      if (!env(root).empty()) cands.push_back(env(root) + "/lib64/libnvrtc.so");
+    cands.push_back("/usr/local/cuda/lib64/libnvrtc.so");
+    void* h = nullptr;
+    for (const auto& c : cands) {
+      h = dlopen(c.c_str(), RTLD_NOW | RTLD_LOCAL);
+      if (h) {
+        n.where = c;
+        break;
+      }
+    }
+    if (!h) {
+      n.where = "NVRTC not found (set VDX_NVRTC to libnvrtc.so)";
+      return;
+    }
+    n.create = reinterpret_cast<decltype(n.create)>(dlsym(h, "nvrtcCreateProgram"));
+    n.compile = reinterpret_cast<decltype(n.compile)>(dlsym(h, "nvrtcCompileProgram"));
+    n.log_size = reinterpret_cast<decltype(n.log_size)>(dlsym(h, "nvrtcGetProgramLogSize"));
+    n.log = reinterpret_cast<decltype(n.log)>(dlsym(h, "nvrtcGetProgramLog"));
+    n.cubin_size = reinterpret_cast<decltype(n.cubin_size)>(dlsym(h, "nvrtcGetCUBINSize"));
+    n.cubin = reinterpret_cast<decltype(n.cubin)>(dlsym(h, "nvrtcGetCUBIN"));
+    n.destroy = reinterpret_cast<decltype(n.destroy)>(dlsym(h, "nvrtcDestroyProgram"));
+    n.error_string = reinterpret_cast<decltype(n.error_string)>(dlsym(h, "nvrtcGetErrorString"));
+    n.ok = n.create && n.compile && n.log_size && n.log && n.cubin_size && n.cubin && n.destroy && n.error_string;
+    if (!n.ok) n.where += ": missing NVRTC entry points";
+  });
+  return n;
+}
+
+// directory holding cuda_fp16.h (the kernel headers include it)
+std::string cuda_include_dir() {
+  std::vector<std::string> cands;
+  if (!env("VDX_CUDA_INCLUDE").empty()) cands.push_back(env("VDX_CUDA_INCLUDE"));
+  for (const char* root : {"CUDA_HOME", "CUDA_PATH"})
+    if (!env(root).empty()) cands.push_back(env(root) + "/include");
+  cands.push_back("/usr/local/cuda/include");
+  for (const auto& c : cands)
+    if (access((c + "/cuda_fp16.h").c_str(), R_OK) == 0) return c;
+  return std::string();
+}
+
+// ---------------------------------------------------------------------------
+// compiled modules: one per (source, device), kept for the process
+// ---------------------------------------------------------------------------
+struct Module {
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t kernel = nullptr;
+};
+std::mutex g_mu;
+std::map<std::pair<std::string, int>, Module> g_modules;
+
+int compile(const std::string& src, int dev, Module* out) {
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_modules.find({src, dev});
+    if (it != g_modules.end()) {
+      *out = it->second;
+      return VDX_OK;
+    }
+  }
+  const Nvrtc& n = nvrtc();
+  if (!n.ok) return set_error(VDX_ERR_UNSUPPORTED, ("map hooks: " + n.where).c_str());
+  const std::string inc = cuda_include_dir();
+  if (inc.empty())
+    return set_error(VDX_ERR_UNSUPPORTED, "map hooks: CUDA headers (cuda_fp16.h) not found; set VDX_CUDA_INCLUDE");
+  int major = 0, minor = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  const std::string arch = "--gpu-architecture=sm_" + std::to_string(major) + std::to_string(minor) + "a";
+  const std::string incopt = "-I" + inc;
+  const char* opts[] = {arch.c_str(), "-std=c++17", "-default-device", "-lineinfo", incopt.c_str()};
+  nvrtcProgram prog = nullptr;
+  nvrtcResult r = n.create(&prog, src.c_str(), "vdx_mapped.cu", kJitHeaderCount, kJitHeaderSources, kJitHeaderNames);
+  if (r != NVRTC_SUCCESS) return set_error(VDX_ERR_CUDA, (std::string("nvrtcCreateProgram: ") + n.error_string(r)).c_str());
+  r = n.compile(prog, int(sizeof(opts) / sizeof(opts[0])), opts);
+  if (r != NVRTC_SUCCESS) {
+    size_t ls = 0;
+    n.log_size(prog, &ls);
+    std::string log(ls, '\0');
+    if (ls) n.log(prog, &log[0]);
+    n.destroy(&prog);
+    if (log.size() > 3000) log.resize(3000);
+    return set_error(VDX_ERR_INVALID, ("map hooks do not compile: " + log).c_str());
+  }
+  size_t cs = 0;
+  n.cubin_size(prog, &cs);
+  std::vector<char> cubin(cs);
+  n.cubin(prog, cubin.data());
+  n.destroy(&prog);
+  Module m;
+  cudaError_t e = cudaLibraryLoadData(&m.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (e == cudaSuccess) e = cudaLibraryGetKernel(&m.kernel, m.lib, "vdx_mapped");
+  if (e != cudaSuccess) {
+    if (m.lib) cudaLibraryUnload(m.lib);
+    return set_error(VDX_ERR_CUDA, (std::string("loading the map kernel: ") + cudaGetErrorString(e)).c_str());
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  auto ins = g_modules.emplace(std::make_pair(src, dev), m);
+  if (!ins.second) cudaLibraryUnload(m.lib);  // compiled concurrently by another thread
+  *out = ins.first->second;
+  return VDX_OK;
+}
+
+}  // namespace
+
+struct vdx_map_plan {
+  MapGeometry g;
+  Module mod;
+  std::string source;
+};
+
+extern "C" {
+
+int vdx_map_plan_create(const vdx_fft_desc* desc, const char* hooks_source, vdx_map_plan** plan) {
+  if (!desc || !hooks_source || !plan) return set_error(VDX_ERR_INVALID, "desc, hooks_source and plan must be non-NULL");
+  *plan = nullptr;
+  if (desc->kind != VDX_KIND_C2C && desc->kind != VDX_KIND_CONV)
+    return set_error(VDX_ERR_INVALID, "map hooks run on C2C or CONV descriptors");
+  if (desc->io_type != desc->compute_type)
+    return set_error(VDX_ERR_INVALID, "map plans: io_type must equal compute_type (the hooks do the I/O)");
+  if (desc->flags != 0) return set_error(VDX_ERR_UNSUPPORTED, "map plans take no desc.flags");
+  vdx_fft_desc d = *desc;
+  d.kernel_type = d.io_type;
+  d.kernel_op = VDX_KOP_MUL_CONJ;
+  auto* p = new vdx_map_plan();
+  int rc = map_plan_geometry(d, &p->g);
+  if (rc != VDX_OK) {
+    delete p;
+    return rc;
+  }
+  const MapGeometry& g = p->g;
+  const int mode = desc->kind == VDX_KIND_CONV ? 2 : (desc->inverse ? 1 : 0);
+  const int maxe = g.f64 ? MaxE<double>::value : MaxE<float>::value;
+  std::string radices;
+  for (size_t i = 0; i < g.radices.size(); ++i) radices += (i ? ", " : "") + std::to_string(g.radices[i]);
+  p->source = std::string("#include \"fft_mapped.cuh\"\n\n") + hooks_source +
+              "\n\nextern \"C\" __global__ void __launch_bounds__(" + std::to_string(g.launch.block.x) +
+              ") vdx_mapped(vdx::FftArgs a, vdx::MapArgs m) {\n  vdx::mapped_body<vdx::FixPlan<" +
+              std::to_string(g.args.pp.n) + ", " + std::to_string(g.args.pp.T) + ", vdx::RList<" + radices + ">, " +
+              std::to_string(maxe) + ">, " + (g.strided ? "true" : "false") + ", " + (g.f64 ? "double" : "float") +
+              ", " + std::to_string(mode) + ", VdxHooks>(a, m);\n}\n";
+  rc = compile(p->source, g.dev, &p->mod);
+  if (rc != VDX_OK) {
+    delete p;
+    return rc;
+  }
+  if (g.launch.smem > 48 * 1024) {
+    cudaError_t e = cudaKernelSetAttributeForDevice(p->mod.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)g.launch.smem, g.dev);
+    if (e != cudaSuccess) {
+      delete p;
+      return set_error(VDX_ERR_CUDA, (std::string("map kernel shared memory: ") + cudaGetErrorString(e)).c_str());
+    }
+  }
+  *plan = p;
+  return VDX_OK;
+}
+
+int vdx_map_plan_destroy(vdx_map_plan* plan) {
+  delete plan;  // the compiled module stays cached for later plans of the same source
+  return VDX_OK;
+}
+
+int vdx_map_exec(const vdx_map_plan* p, const vdx_map_args* args, void* stream) {
+  if (!p || !args) return set_error(VDX_ERR_INVALID, "plan and args must be non-NULL");
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != p->g.dev) return set_error(VDX_ERR_INVALID, "map plan was created on another device");
+  FftArgs a = p->g.args;
+  MapArgs m;
+  std::memcpy(&m, args, sizeof(m));
+  void* kargs[] = {&a, &m};
+  const Launch& l = p->g.launch;
+  cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(p->mod.kernel), l.grid, l.block, kargs, l.smem,
+                                   reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return set_error(VDX_ERR_CUDA, (std::string("map kernel launch: ") + cudaGetErrorString(e)).c_str());
+  return VDX_OK;
+}
+
+int vdx_map_plan_source(const vdx_map_plan* p, char* buf, size_t n) {
+  if (!p || !buf || n == 0) return set_error(VDX_ERR_INVALID, "plan and a non-empty buffer are required");
+  std::snprintf(buf, n, "%s", p->source.c_str());
+  return p->source.size() < n ? VDX_OK : set_error(VDX_ERR_INVALID, "buffer too small for the source");
+}
+
+}  // extern "C"

@@ -1107,6 +1107,32 @@ int autotune_plan(const vdx_fft_desc& d0, vdx_plan** plan) {
 
 }  // namespace
 
+namespace vdx {
+
+int map_plan_geometry(const vdx_fft_desc& d, MapGeometry* g) {
+  Tune t;
+  t.fourstep = 0;  // one CTA per transform wherever it fits
+  t.fixed = 0;
+  vdx_plan* p = nullptr;
+  const int rc = create_plan(&d, t, &p);
+  if (rc != VDX_OK) return rc;
+  if (p->fourstep || p->bluestein || p->radices.empty()) {
+    delete p;
+    return fail(VDX_ERR_UNSUPPORTED, "map hooks run on axes of at most 16384 points whose transform fits one CTA");
+  }
+  g->args = p->args;
+  g->launch = p->launch;
+  g->radices = p->radices;
+  g->strided = p->strided;
+  g->f64 = p->f64;
+  g->N = p->N;
+  g->dev = p->dev;
+  delete p;
+  return VDX_OK;
+}
+
+}  // namespace vdx
+
 extern "C" {
 
 int vdx_version(void) { return 100; }

@@ -10,13 +10,45 @@
 // in double precision.
 #pragma once
 
+#ifdef __CUDACC_RTC__
+// runtime-compiled map kernels (NVRTC): no host headers
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+typedef unsigned short uint16_t;
+typedef int int32_t;
+typedef unsigned int uint32_t;
+typedef long long int64_t;
+typedef unsigned long long uint64_t;
+#else
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
-#include <type_traits>
+#endif
 
 namespace vdx {
+
+// the few type traits the kernels use, here so that the same headers compile
+// under NVRTC, which has no standard library
+template <class T, T V>
+struct IntConst {
+  static constexpr T value = V;
+  constexpr operator T() const { return V; }
+};
+using TrueT = IntConst<bool, true>;
+using FalseT = IntConst<bool, false>;
+template <bool B, class A, class C>
+struct Cond {
+  using type = A;
+};
+template <class A, class C>
+struct Cond<false, A, C> {
+  using type = C;
+};
+template <class A, class C>
+struct Same : FalseT {};
+template <class A>
+struct Same<A, A> : TrueT {};
 
 // ---------------------------------------------------------------------------
 // complex value in registers

@@ -5,7 +5,11 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "fft_kernels.cuh"
+
+struct vdx_fft_desc;  // include/vdx.h
 
 namespace vdx {
 
@@ -154,6 +158,20 @@ inline cudaError_t enqueue(K kernel, const Launch& l, Args... args) {
   kernel<<<l.grid, l.block, l.smem, l.stream>>>(args...);
   return cudaGetLastError();
 }
+
+// Geometry of a single-CTA-per-transform plan (no four-step, no Bluestein)
+// for the run-time compiled map kernels of jit.cu: the planner's pass plan,
+// launch shape and twiddle table for the descriptor's axis.
+struct MapGeometry {
+  FftArgs args;
+  Launch launch;
+  std::vector<int> radices;
+  bool strided;
+  bool f64;
+  int N;
+  int dev;
+};
+int map_plan_geometry(const ::vdx_fft_desc& d, MapGeometry* g);
 
 // error reporting and argument checks shared by the C entry points
 int set_error(int code, const char* msg);

@@ -212,7 +212,13 @@ def fft(
         if output_map is not None and output_type is not None:
             raise ValueError("output_type cannot be provided when output_map is used")
         outs, ins, _ = _split_buffers(buffers, input_map, output_map)
-        out_buf, out_kind, in_buf, in_kind = _io_ends(outs, ins, input_map, output_map)
+        try:
+            out_buf, out_kind, in_buf, in_kind = _io_ends(outs, ins, input_map, output_map)
+        except NotImplementedError as menu:
+            _jit_transform(outs, ins, [], input_map, output_map, None, False, buffer_shape, axis, inverse,
+                           bool(inverse and normalize_inverse), compute_type, input_signal_range, graph, print_shader,
+                           menu)
+            return
         io = []
         if output_map is None:
             io.append(out_buf.var_type)
@@ -461,8 +467,15 @@ def _convolve_mapped(buffers, kernel_map, buffer_shape, graph, axis, normalize, 
     from . import maps as M
 
     outs, ins, kers = _split_buffers(buffers, input_map, output_map, kernel_map, conv=True)
-    out_buf, out_kind, in_buf, in_kind = _io_ends(outs, ins, input_map, output_map)
-    km = M.classify_kernel(kernel_map) if kernel_map is not None else M.KernelMap("conj_mul", 0, kers[0].var_type)
+    try:
+        out_buf, out_kind, in_buf, in_kind = _io_ends(outs, ins, input_map, output_map)
+        km = M.classify_kernel(kernel_map) if kernel_map is not None else M.KernelMap("conj_mul", 0,
+                                                                                     kers[0].var_type)
+    except NotImplementedError as menu:
+        _jit_transform(outs, ins, kers, input_map, output_map, kernel_map, True, buffer_shape, axis, False,
+                       bool(normalize), compute_type, input_signal_range, graph, False, menu,
+                       kernel_inner_only=kernel_inner_only)
+        return
     io = []
     if output_map is None:
         io.append(out_buf.var_type)
@@ -534,6 +547,13 @@ def _convolve_multi(buffers, kernel_map, kernel_num, buffer_shape, graph, axis, 
     from . import maps as M
 
     outs, ins, kers = _split_buffers(buffers, input_map, output_map, kernel_map, conv=True)
+    try:
+        _classify_multi(input_map, output_map, kernel_map)
+    except NotImplementedError as menu:
+        _jit_transform(outs, ins, kers, input_map, output_map, kernel_map, True, buffer_shape, axis, False,
+                       bool(normalize), compute_type, input_signal_range, graph, False, menu,
+                       kernel_inner_only=kernel_inner_only, kernel_num=kernel_num)
+        return
     if output_map is not None:
         om = M.classify_output(output_map)
         if om.kind != "complex":
@@ -593,6 +613,91 @@ def _convolve_multi(buffers, kernel_map, kernel_num, buffer_shape, graph, axis, 
             plan.exec(src, out_ptr + k * ostride * es, k_ptr + k * kstride * es, s)
 
     _record(graph, launch, (in_buf, out_buf, kbuf, stage))
+
+
+def _classify_multi(input_map, output_map, kernel_map) -> None:
+    """Raises NotImplementedError when a multi-kernel convolution's maps are
+    outside what the fused multi-kernel launch implements."""
+    from . import maps as M
+
+    if output_map is not None and M.classify_output(output_map).kind != "complex":
+        raise NotImplementedError("multi-kernel convolutions write complex outputs")
+    if input_map is not None and M.classify_input(input_map).kind != "complex":
+        raise NotImplementedError("multi-kernel convolutions read complex inputs")
+    if kernel_map is not None and M.classify_kernel(kernel_map).kind not in ("conj_mul", "mul"):
+        raise NotImplementedError("multi-kernel convolutions take a (conjugate) product with a kernel buffer")
+
+
+def _first_buffer(*groups):
+    for g in groups:
+        for b in g or ():
+            if isinstance(b, Buffer):
+                return b
+    raise ValueError("at least one Buffer argument is required")
+
+
+def _jit_transform(outs, ins, kers, input_map, output_map, kernel_map, conv, buffer_shape, axis, inverse, normalize,
+                   compute_type, input_signal_range, graph, print_shader, menu_error, kernel_inner_only=False,
+                   kernel_num=1):
+    """An FFT or convolution whose maps are outside the functor menu: the
+    maps are lowered to a C++ hooks struct and compiled with NVRTC into the
+    FFT kernel template (vkdispatch_gb300/fft/jit.py).  A multi-kernel
+    convolution runs one launch per kernel index; when the output may
+    overwrite the signal it reads, the signal is read from a copy, so every
+    kernel sees the original signal."""
+    import torch
+
+    from . import jit as J
+
+    io = []
+    if output_map is None:
+        io.append(outs[0].var_type)
+    if input_map is None:
+        io.append((ins[0] if ins else outs[0]).var_type)
+    if conv and kernel_map is None:
+        io.append(kers[0].var_type)
+    for t in io:
+        if t not in _PRECISION_ORDER:
+            raise ValueError(f"buffers without a map must be complex (got {t.name})")
+    compute = resolve_compute_precision(io, compute_type)
+    code = _compute_code(None, compute)
+    first = _first_buffer(outs, ins, kers)
+    shape = tuple(int(x) for x in (buffer_shape if buffer_shape is not None else first.shape))
+    ax = _norm_axis(axis, len(shape))
+    total, slab = math.prod(shape), math.prod(shape[ax:])
+    bslab = 0
+    if conv and kernel_map is None:
+        kb = kers[0]
+        if kernel_inner_only or kb.size < total:
+            if kb.size < slab:
+                raise ValueError(f"kernel buffer of {kb.size} elements is smaller than the signal ({total})")
+            bslab = slab
+    stage = stage_src = None
+    if kernel_num > 1 and input_map is None:
+        # the signal the default load reads, copied when an output buffer aliases it
+        src = ins[0] if ins else outs[0]
+        if any(isinstance(b, Buffer) and b.ptr == src.ptr for b in outs):
+            stage, stage_src = Buffer(src.shape, src.var_type), src
+            ins = [stage]
+    try:
+        spec = J.build_hooks(outs, ins, kers, input_map, output_map, kernel_map, conv, bslab)
+    except NotImplementedError as e:
+        raise NotImplementedError(f"{menu_error}; and the map-hook compiler: {e}") from e
+    plan = J.get_plan(shape, ax, conv, inverse, 1 if normalize else 0, code, _signal(input_signal_range, shape[ax]),
+                      spec.source)
+    if print_shader:
+        print(plan.source())
+    slots = spec.slots
+
+    def launch(s):
+        if stage is not None:
+            n = stage_src.tensor.numel()
+            with torch.cuda.stream(torch.cuda.ExternalStream(s) if s else torch.cuda.current_stream()):
+                stage.tensor.reshape(-1)[:n].copy_(stage_src.tensor.reshape(-1), non_blocking=True)
+        for k in range(kernel_num):
+            plan.exec(J.make_args(slots, k), s)
+
+    _record(graph, launch, tuple(slots.buffers) + ((stage,) if stage is not None else ()))
 
 
 def convolve2D(buffer: Buffer, kernel: Buffer, kernel_map=None, buffer_shape=None, graph=None, print_shader=False,

@@ -3,8 +3,11 @@ the recognition of user map functions (vkdispatch/fft/io_manager.py:23-37,
 vkdispatch/shader/map.py:10-68).
 
 A map function is called once with symbolic buffers and read/write-op
-objects that record what it does.  The record is matched against the menu
-libvdx implements; anything else raises NotImplementedError naming the map.
+objects that record what it does.  The record is first matched against the
+menu of maps that libvdx's ahead-of-time kernels implement; a map outside
+the menu is lowered to C++ and compiled at run time instead
+(vkdispatch_gb300/fft/jit.py), and only constructs that compiler lacks raise
+NotImplementedError naming the map.
 
   input maps   read_op().read_from_buffer(buf)           complex load of buf's type
                register.real = buf[io_index]; .imag = 0  real load (imaginary 0)
@@ -33,8 +36,13 @@ from .. import dtypes as dt
 _tls = threading.local()
 
 
-class TraceRegister:
+class TraceRegister(vc.Sym):
+    """An FFT register (or a new_register temporary) while a map is traced:
+    arithmetic on it builds expressions over ``reg(name)``; assignments to
+    ``.real``, ``.imag`` or ``[:]`` are recorded as events."""
+
     def __init__(self, name: str, events: list):
+        vc.Sym.__init__(self, "reg", name)
         object.__setattr__(self, "_name", name)
         object.__setattr__(self, "_events", events)
 
@@ -53,6 +61,14 @@ class TraceRegister:
     @imag.setter
     def imag(self, value):
         self._events.append(("set_imag", self._name, value))
+
+    @property
+    def x(self):
+        return self.real
+
+    @property
+    def y(self):
+        return self.imag
 
     def __setitem__(self, key, value):
         self._events.append(("set", self._name, value))
@@ -75,10 +91,18 @@ class _TraceBuffer:
         self._events = events
 
     def __getitem__(self, idx):
-        return vc.Sym("load", self.index)
+        return vc.Sym("load", self.index, idx)
 
     def __setitem__(self, idx, value):
-        self._events.append(("store", self.index, value))
+        self._events.append(("store", self.index, value, idx))
+
+
+class _TraceScalar(vc.Sym):
+    """A scalar map argument (``vc.Var[...]``)."""
+
+    def __init__(self, index: int, var_type):
+        vc.Sym.__init__(self, "scalar", index)
+        self.var_type = var_type
 
 
 class _TraceOp:
@@ -92,11 +116,11 @@ class _TraceOp:
     def read_from_buffer(self, buffer, register=None, io_index=None):
         name = register._name if isinstance(register, TraceRegister) else "reg"
         stride = kernel_stride(io_index)
-        self._events.append(("read", buffer.index, name, stride is not None, stride or 0))
+        self._events.append(("read", buffer.index, name, stride is not None, stride or 0, io_index))
 
     def write_to_buffer(self, buffer, register=None, io_index=None):
         stride = kernel_stride(io_index)
-        self._events.append(("write", buffer.index, stride is not None, stride or 0))
+        self._events.append(("write", buffer.index, stride is not None, stride or 0, register, io_index))
 
 
 def mapped_kernel_index():
@@ -143,19 +167,22 @@ def write_op():
     return op
 
 
-def new_trace_register(var_type):
+def new_trace_register(var_type, *args):
     events = getattr(_tls, "events", None)
     if events is None:
         raise ValueError("new_register is only available while a map function is traced")
     n = getattr(_tls, "nreg", 0)
     _tls.nreg = n + 1
-    return TraceRegister(f"tmp{n}", events)
+    name = f"tmp{n}"
+    events.append(("new", name, var_type, args))
+    return TraceRegister(name, events)
 
 
 def _trace(mf, role: str):
     events: list = []
     types = mf.input_dtypes()
-    bufs = [_TraceBuffer(i, t, events) for i, t in enumerate(types)]
+    scalar = mf.arg_is_scalar()
+    bufs = [_TraceScalar(i, t) if sc else _TraceBuffer(i, t, events) for i, (t, sc) in enumerate(zip(types, scalar))]
     _tls.events, _tls.nreg = events, 0
     _tls.kidx = vc.Sym("kidx")
     _tls.read = _TraceOp(events) if role in ("input", "kernel") else None
@@ -177,6 +204,36 @@ def _has(expr, op, arg=None) -> bool:
     if expr.op == op and (arg is None or arg in expr.args):
         return True
     return any(_has(a, op, arg) for a in expr.args)
+
+
+def _menu_events(ev):
+    """The events the menu matchers look at: new_register temporaries
+    declared without an initial value carry no operation of their own."""
+    return [e for e in ev if not (e[0] == "new" and not e[3])]
+
+
+def _loads_at_io(expr) -> bool:
+    """Every buffer load inside expr reads at io_index itself."""
+    if not isinstance(expr, vc.Sym):
+        return True
+    if expr.op == "load":
+        return len(expr.args) > 1 and isinstance(expr.args[1], vc.Sym) and expr.args[1].op == "io_index"
+    return all(_loads_at_io(a) for a in expr.args)
+
+
+def _is_reg_real(expr) -> bool:
+    """expr is the FFT register's real part, possibly cast."""
+    while isinstance(expr, vc.Sym) and expr.op == "cast":
+        expr = expr.args[0]
+    return isinstance(expr, vc.Sym) and expr.op == "reg_real" and expr.args == ("reg",)
+
+
+def _plain_cast_of_load(expr, buf) -> bool:
+    """expr is buf[io_index], possibly cast: the menu's real-input load."""
+    while isinstance(expr, vc.Sym) and expr.op == "cast":
+        expr = expr.args[0]
+    return (isinstance(expr, vc.Sym) and expr.op == "load" and expr.args[0] == buf
+            and isinstance(expr.args[1], vc.Sym) and expr.args[1].op == "io_index")
 
 
 def _is_zero(expr) -> bool:
@@ -203,6 +260,7 @@ class KernelMap:
 
 def classify_input(mf) -> IoMap:
     ev, types = _trace(mf, "input")
+    ev = _menu_events(ev)
     name = mf.func.__name__
     if len(ev) == 1 and ev[0][0] == "read" and ev[0][2] == "reg" and ev[0][3] and ev[0][4] == 0:
         i = ev[0][1]
@@ -212,20 +270,23 @@ def classify_input(mf) -> IoMap:
     sets = {e[0]: e for e in ev if e[1] == "reg"}
     if len(ev) == 2 and set(sets) == {"set_real", "set_imag"} and _is_zero(sets["set_imag"][2]):
         loads = [a for a in range(len(types)) if _has(sets["set_real"][2], "load", a)]
-        if len(loads) == 1 and types[loads[0]] in (dt.float32, dt.float64):
+        if (len(loads) == 1 and types[loads[0]] in (dt.float32, dt.float64)
+                and _plain_cast_of_load(sets["set_real"][2], loads[0])):
             return IoMap("real", loads[0], types[loads[0]])
     raise NotImplementedError(f"input map {name} is not in the supported map menu: {ev}")
 
 
 def classify_output(mf) -> IoMap:
     ev, types = _trace(mf, "output")
+    ev = _menu_events(ev)
     name = mf.func.__name__
-    if len(ev) == 1 and ev[0][0] == "write" and ev[0][2]:
+    if len(ev) == 1 and ev[0][0] == "write" and ev[0][2] and ev[0][4] is None:
         i = ev[0][1]
         if not types[i].is_complex:
             raise NotImplementedError(f"output map {name}: write_to_buffer needs a complex buffer")
         return IoMap("complex", i, types[i], ev[0][3])
-    if len(ev) == 1 and ev[0][0] == "store" and _has(ev[0][2], "reg_real", "reg"):
+    if (len(ev) == 1 and ev[0][0] == "store" and _is_reg_real(ev[0][2])
+            and isinstance(ev[0][3], vc.Sym) and ev[0][3].op == "io_index"):
         i = ev[0][1]
         if types[i] in (dt.float32, dt.float64):
             return IoMap("real", i, types[i])
@@ -234,6 +295,7 @@ def classify_output(mf) -> IoMap:
 
 def classify_kernel(mf) -> KernelMap:
     ev, types = _trace(mf, "kernel")
+    ev = _menu_events(ev)
     name = mf.func.__name__
     if not ev:
         return KernelMap("identity", None, None)
@@ -251,6 +313,7 @@ def classify_kernel(mf) -> KernelMap:
         prod = ev[0][2]
         if isinstance(prod, vc.Sym) and prod.op == "cmul" and _has(prod.args[1], "to_complex"):
             loads = [a for a in range(len(types)) if _has(prod.args[1], "load", a)]
-            if len(loads) == 1 and types[loads[0]] in (dt.float32, dt.float64):
+            if (len(loads) == 1 and types[loads[0]] in (dt.float32, dt.float64) and _loads_at_io(prod.args[1])
+                    and isinstance(prod.args[0], TraceRegister) and prod.args[0]._name == "reg"):
                 return KernelMap("real_scale", loads[0], types[loads[0]])
     raise NotImplementedError(f"kernel map {name} is not in the supported map menu: {ev}")

@@ -67,7 +67,8 @@ def _trace_map(func, in_types) -> int:
         raise NotImplementedError(f"map {func.__name__} could not be traced: {e}") from e
 
     def is_load(x):
-        return isinstance(x, vc.Sym) and x.op == "load" and x.args == (0,)
+        return (isinstance(x, vc.Sym) and x.op == "load" and x.args[:1] == (0,)
+                and (len(x.args) == 1 or isinstance(x.args[1], vc._IoIndex)))
 
     if len(in_types) != 1:
         raise NotImplementedError(f"map {func.__name__}: maps over more than one buffer are not in the menu")
@@ -124,6 +125,9 @@ def _resolve_annotation(a):
     m = re.fullmatch(r"\s*(?:[\w.]*\.)?(?:Buff|Buffer)\[\s*(?:[\w.]*\.)?(\w+)\s*\]\s*", a)
     if m and _named_dtype(m.group(1)) is not None:
         return vc.Buffer[_named_dtype(m.group(1))]
+    m = re.fullmatch(r"\s*(?:[\w.]*\.)?Var\[\s*(?:[\w.]*\.)?(\w+)\s*\]\s*", a)
+    if m and _named_dtype(m.group(1)) is not None:
+        return vc.Var[_named_dtype(m.group(1))]
     m = re.fullmatch(r"\s*(?:[\w.]*\.)?(\w+)\s*", a)
     if m and _named_dtype(m.group(1)) is not None:
         return _named_dtype(m.group(1))
@@ -142,6 +146,10 @@ class MappingFunction:
         if input_types is None:
             input_types = [_resolve_annotation(p.annotation) for p in sig.parameters.values()]
         self.buffer_types = list(input_types)
+
+    def arg_is_scalar(self) -> List[bool]:
+        """Per argument: a scalar (``vc.Var[...]``) rather than a buffer."""
+        return [bool(getattr(t, "is_scalar", False)) for t in self.buffer_types]
 
     def input_dtypes(self) -> List[dt.dtype]:
         out = []
