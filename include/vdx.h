@@ -372,6 +372,9 @@ int vdx_reduce_noalloc(int op, int map, int in_type, const void* in, int64_t n, 
 #define VDX_MAP_MAX_SCALARS 8
 typedef struct vdx_map_args {
   void* buffers[VDX_MAP_MAX_BUFFERS];  /* device pointers the hooks index */
+  int64_t counts[VDX_MAP_MAX_BUFFERS]; /* elements each may be indexed with: an index outside
+                                          [0, count) loads 0, skips its store and sets the
+                                          plan's status (vdx_map_plan_status) */
   double fscalars[VDX_MAP_MAX_SCALARS]; /* floating-point map arguments */
   int64_t iscalars[VDX_MAP_MAX_SCALARS]; /* integer map arguments */
   int64_t kernel_index;                /* mapped_kernel_index() of a multi-kernel convolution */
@@ -383,6 +386,9 @@ int vdx_map_plan_destroy(vdx_map_plan* plan);
 int vdx_map_exec(const vdx_map_plan* plan, const vdx_map_args* args, void* stream);
 /* The full source NVRTC compiled for the plan (hooks and instantiation). */
 int vdx_map_plan_source(const vdx_map_plan* plan, char* buf, size_t n);
+/* 1 when a launch of the plan indexed a map buffer out of range, else 0
+ * (synchronous read; reset != 0 clears it). */
+int vdx_map_plan_status(const vdx_map_plan* plan, int* status, int reset);
 
 #ifdef __cplusplus
 }

@@ -1,6 +1,6 @@
 """Bluestein (chirp-z) transforms for lengths with prime factors above 13
-(VDX_FFT_FLAG_BLUESTEIN, vd.fft.bluestein()), which the reference rejects
-(vkdispatch/fft/prime_utils.py:6-10), against FP64 numpy.fft.
+(VDX_FFT_FLAG_BLUESTEIN; on by default in vd.fft), which the reference
+rejects (vkdispatch/fft/prime_utils.py:6-10), against FP64 numpy.fft.
 
 Tolerance: the transform is a length-M convolution (M = the power of two
 >= 2N - 1) between two chirp multiplications, so fp32 compute is held to
@@ -67,10 +67,35 @@ def test_bf16_storage():
     assert rel_l2(buf.read(0), np.fft.fft(q, axis=1)) < 5e-3
 
 
-def test_limits_and_default_refusal():
-    b = vd.Buffer((2, 17), vd.complex64)
+def test_default_on_and_refusal_on_request():
+    rng = np.random.default_rng(41)
+    x = crandn(rng, (2, 17))
+    b = vd.asbuffer(x)
+    vd.fft.fft(b)  # Bluestein by default
+    assert rel_l2(b.read(0), np.fft.fft(x.astype(np.complex128), axis=1)) <= 3 * tol_fp32(_m(17))
+    with vd.fft.bluestein(False), pytest.raises(ValueError):
+        vd.fft.fft(vd.Buffer((2, 17), vd.complex64))  # the reference's behaviour
     with pytest.raises(ValueError):
-        vd.fft.fft(b)  # the reference's behaviour without the flag
-    big = vd.Buffer((1, 8209), vd.complex64)  # prime: needs a 32768-point convolution
-    with vd.fft.bluestein(), pytest.raises(ValueError):
-        vd.fft.fft(big)
+        vd.fft.fft(vd.Buffer((1, 8209), vd.complex128))  # fp64: single-CTA convolutions only (M <= 8192)
+
+
+@pytest.mark.parametrize("n,rows", [(8209, 3), (16411, 2), (65537, 1)])
+def test_long_lengths_through_four_step(n, rows):
+    """M > 16384: the convolution runs as a four-step forward transform, a
+    spectrum product and a four-step inverse."""
+    rng = np.random.default_rng(n)
+    x = crandn(rng, (rows, n))
+    b = vd.asbuffer(x)
+    vd.fft.fft(b)
+    got = b.read(0)
+    assert rel_l2(got, np.fft.fft(x.astype(np.complex128), axis=1)) <= 3 * tol_fp32(_m(n))
+    vd.fft.ifft(b)
+    assert rel_l2(b.read(0), x) <= 6 * tol_fp32(_m(n))
+
+
+def test_long_strided_axis():
+    rng = np.random.default_rng(43)
+    x = crandn(rng, (10007, 4))
+    b = vd.asbuffer(x)
+    vd.fft.fft(b, axis=0)
+    assert rel_l2(b.read(0), np.fft.fft(x.astype(np.complex128), axis=0)) <= 3 * tol_fp32(_m(10007))

@@ -93,11 +93,16 @@ def test_index_expression_outside_the_menu_is_compiled():
         op.read_from_buffer(kernels, register=kv, io_index=op.io_index * 2)
         op.register[:] = vc.mult_complex(op.register, kv.conjugate())
 
+    from vkdispatch_gb300.fft import jit
+
     rng = np.random.default_rng(21)
     x = (rng.standard_normal((2, 32)) + 1j * rng.standard_normal((2, 32))).astype(np.complex64)
     k = (rng.standard_normal((4, 32)) + 1j * rng.standard_normal((4, 32))).astype(np.complex64)
     b = vd.asbuffer(x)
-    vd.fft.convolve(b, b, vd.asbuffer(k), kernel_map=vd.map(strided_map), kernel_num=2)
+    jit.out_of_range(reset=True)
+    # no input or output map: the output buffer, then the kernel map's buffer
+    vd.fft.convolve(b, vd.asbuffer(k), kernel_map=vd.map(strided_map), kernel_num=2)
+    assert not jit.out_of_range()
     k2 = k.reshape(-1)[::2].reshape(2, 32).astype(np.complex128)
     want = np.fft.ifft(np.fft.fft(x.astype(np.complex128), axis=1) * np.conj(k2), axis=1)
     assert np.linalg.norm(b.read(0) - want) / np.linalg.norm(want) <= 2 * 5e-7 * 5
@@ -198,3 +203,31 @@ def test_kernel_bank_broadcast_over_batches(N):
     s = np.fft.fft(x.astype(np.complex128), axis=1)
     for k in range(K):
         assert rel_l2(got[k], np.fft.ifft(s * np.conj(bank[k])[None, :], axis=1)) <= 2 * tol_fp32(N)
+
+
+def test_out_of_range_map_index_is_caught():
+    """A kernel map indexing past its buffer (io_index * 2 into a buffer of
+    the signal's size) never touches memory outside it: the bounds check of
+    the compiled hooks loads zero there and reports through the plan's
+    status word."""
+    from vkdispatch_gb300.fft import jit
+
+    def strided_map(kernels: vc.Buffer[vd.complex64]):
+        op = vd.fft.read_op()
+        kv = vc.new_register(vd.complex64)
+        op.read_from_buffer(kernels, register=kv, io_index=op.io_index * 2)
+        op.register[:] = vc.mult_complex(op.register, kv.conjugate())
+
+    rng = np.random.default_rng(22)
+    x = (rng.standard_normal((2, 32)) + 1j * rng.standard_normal((2, 32))).astype(np.complex64)
+    k = (rng.standard_normal((2, 32)) + 1j * rng.standard_normal((2, 32))).astype(np.complex64)
+    b = vd.asbuffer(x)
+    jit.out_of_range(reset=True)
+    vd.fft.convolve(b, vd.asbuffer(k), kernel_map=vd.map(strided_map))
+    assert jit.out_of_range()
+    kk = np.zeros(64, np.complex128)
+    kk[:32] = k.reshape(-1)[::2]  # indices 64.. read as zero
+    want = np.fft.ifft(np.fft.fft(x.astype(np.complex128), axis=1) * np.conj(kk.reshape(2, 32)), axis=1)
+    assert np.linalg.norm(b.read(0) - want) / np.linalg.norm(want) <= 2 * 5e-7 * 5
+    assert not jit.out_of_range()  # the check above reset it
+

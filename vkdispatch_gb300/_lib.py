@@ -62,6 +62,7 @@ EXPORTED = (
     "vdx_map_plan_destroy",
     "vdx_map_exec",
     "vdx_map_plan_source",
+    "vdx_map_plan_status",
 )
 VDX_REDUCE_NOALLOC_SCRATCH_BYTES = 1048576
 
@@ -103,6 +104,7 @@ class MapArgs(ctypes.Structure):
 
     _fields_ = [
         ("buffers", ctypes.c_void_p * 8),
+        ("counts", ctypes.c_int64 * 8),
         ("fscalars", ctypes.c_double * 8),
         ("iscalars", ctypes.c_int64 * 8),
         ("kernel_index", ctypes.c_int64),
@@ -177,6 +179,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.vdx_map_plan_destroy.argtypes = [vp]
     lib.vdx_map_exec.restype = i32
     lib.vdx_map_exec.argtypes = [vp, ctypes.POINTER(MapArgs), vp]
+    lib.vdx_map_plan_status.restype = i32
+    lib.vdx_map_plan_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int), i32]
     lib.vdx_map_plan_source.restype = i32
     lib.vdx_map_plan_source.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     lib.vdx_reduce_noalloc.restype = i32

@@ -1,10 +1,13 @@
 """Device buffers with the reference's Buffer / RFFTBuffer surface
 (vkdispatch/base/buffer.py:40-466), backed by PyTorch device memory.
 
-A Buffer owns (or aliases) one contiguous torch tensor on the current CUDA
-device; ``ptr`` is what the C ABI receives.  ``from_cuda_array`` aliases any
-object exposing ``__cuda_array_interface__`` without copying, with the
-reference's checks: C-contiguous, dtype match, read-only flag.
+A Buffer owns (or aliases) one torch tensor on the current CUDA device;
+``ptr`` is what the C ABI receives.  ``from_cuda_array`` aliases any object
+exposing ``__cuda_array_interface__`` without copying, with the reference's
+checks: C-contiguous (unless ``require_contiguous=False``), dtype match,
+read-only flag.  A buffer over a non-contiguous array records its element
+strides (``strides``); the FFT functions then address it through its
+strides instead of assuming C order.
 """
 
 from __future__ import annotations
@@ -50,6 +53,7 @@ class Buffer:
         self.size = size
         self.writable = writable
         self._keepalive = None
+        self.strides = None  # element strides of a non-contiguous external array, else None (C order)
         lane_shape = shape + ((var_type.lanes,) if var_type.lanes > 1 else ())
         if external is None:
             self._t = torch.empty(lane_shape, dtype=var_type.torch_dtype, device=_device())
@@ -68,6 +72,7 @@ class Buffer:
         b.size = math.prod(shape)
         b.writable = True
         b._keepalive = None
+        b.strides = None
         lane_shape = shape + ((var_type.lanes,) if var_type.lanes > 1 else ())
         b._t = torch.empty(lane_shape, dtype=var_type.torch_dtype, device=_device())
         return b
@@ -76,6 +81,10 @@ class Buffer:
     @property
     def ptr(self) -> int:
         return int(self._t.data_ptr())
+
+    @property
+    def contiguous(self) -> bool:
+        return self.strides is None
 
     @property
     def tensor(self) -> torch.Tensor:
@@ -187,22 +196,30 @@ def from_cuda_array(
         var_type = inferred
     if var_type != inferred:
         raise ValueError(f"CAI dtype ({iface['typestr']}) does not match requested dtype ({var_type.name}).")
-    if require_contiguous:
-        strides = iface.get("strides")
-        if strides is not None:
-            expected, s = [], np.dtype(inferred.np_dtype).itemsize
-            for d in reversed(shape):
-                expected.insert(0, s)
-                s *= d
-            if tuple(int(x) for x in strides) != tuple(expected):
+    strides = iface.get("strides")
+    elem_strides = None
+    if strides is not None:
+        itemsize = np.dtype(inferred.np_dtype).itemsize
+        expected, s = [], itemsize
+        for d in reversed(shape):
+            expected.insert(0, s)
+            s *= d
+        strides = tuple(int(x) for x in strides)
+        if strides != tuple(expected) and not all(d == 1 or st == ex for d, st, ex in zip(shape, strides, expected)):
+            if require_contiguous:
                 raise ValueError("Only contiguous C-order CUDA arrays are supported in from_cuda_array().")
+            if any(st < 0 or st % itemsize for st in strides):
+                raise ValueError("strided CUDA arrays need non-negative strides that are multiples of the item size")
+            elem_strides = tuple(st // itemsize for st in strides)
     buf_writable = (not read_only) if writable is None else bool(writable)
     if buf_writable and read_only:
         raise ValueError("Requested writable=True for a read-only CUDA array.")
     t = torch.as_tensor(obj, device=_device())
     if int(t.data_ptr()) != int(data[0]):
         raise ValueError("could not alias the CUDA array without a copy")
-    return Buffer(shape, var_type, external=(t, obj if keepalive else None), writable=buf_writable)
+    buf = Buffer(shape, var_type, external=(t, obj if keepalive else None), writable=buf_writable)
+    buf.strides = elem_strides
+    return buf
 
 
 class RFFTBuffer(Buffer):

@@ -9,7 +9,9 @@
 //   b[m] = conj(w[m]) for m < N, b[M - m] = conj(w[m]) for 0 < m < N, 0 otherwise;
 //   X[k] = w[k] * IFFT_M(FFT_M(a) * FFT_M(b))[k].
 // The middle step is one fused convolution launch (k_conv multiplies by the
-// conjugate of its kernel, so the kernel passed is conj(FFT_M(b))).  The chirp
+// conjugate of its kernel, so the kernel passed is conj(FFT_M(b))) while M
+// fits one CTA per transform; longer M run it as a four-step forward
+// transform, a spectrum product (k_bs_mul) and a four-step inverse.  The chirp
 // is built in FP64 from the exact integer n^2 mod 2N, so no angle grows with n.
 #include <cuda_runtime.h>
 
@@ -85,6 +87,16 @@ __global__ void k_bs_out(const Cx<Re>* __restrict__ ws, S* __restrict__ y, const
   }
 }
 
+// ws (outer, M, inner) *= conj(K[m][i]): the spectrum product of the long
+// (four-step) form, where the convolution is two separate transforms
+template <class Re>
+__global__ void k_bs_mul(Cx<Re>* __restrict__ ws, const Cx<Re>* __restrict__ K, long long outer, long long slab) {
+  const long long total = outer * slab;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x)
+    ws[e] = cmulc(ws[e], K[e % slab]);
+}
+
 unsigned grid_for(long long total, int threads) {
   long long g = (total + threads - 1) / threads;
   return (unsigned)std::min<long long>(std::max<long long>(g, 1), 152 * 32);
@@ -125,6 +137,16 @@ cudaError_t launch_conj_slab(void* K, const void* B, int M, long long inner, boo
   const unsigned g = (unsigned)((total + TH - 1) / TH);
   if (f64) k_conj_slab<double><<<g, TH, 0, s>>>(static_cast<Cx<double>*>(K), static_cast<const Cx<double>*>(B), M, inner);
   else k_conj_slab<float><<<g, TH, 0, s>>>(static_cast<Cx<float>*>(K), static_cast<const Cx<float>*>(B), M, inner);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bluestein_mul(void* ws, const void* K, long long outer, int M, long long inner, bool f64,
+                                 cudaStream_t s) {
+  constexpr int TH = 256;
+  const long long slab = (long long)M * inner;
+  const unsigned g = grid_for(outer * slab, TH);
+  if (f64) k_bs_mul<double><<<g, TH, 0, s>>>(static_cast<Cx<double>*>(ws), static_cast<const Cx<double>*>(K), outer, slab);
+  else k_bs_mul<float><<<g, TH, 0, s>>>(static_cast<Cx<float>*>(ws), static_cast<const Cx<float>*>(K), outer, slab);
   return cudaGetLastError();
 }
 

@@ -24,27 +24,38 @@ constexpr int kMapMaxScalars = 8;
 
 struct MapArgs {
   void* buf[kMapMaxBuffers];
-  double fs[kMapMaxScalars];     // floating-point scalar map arguments
-  long long is[kMapMaxScalars];  // integer scalar map arguments
-  long long kidx;                // mapped_kernel_index() of a multi-kernel convolution
+  long long count[kMapMaxBuffers];  // elements each buffer slot may be indexed with
+  double fs[kMapMaxScalars];        // floating-point scalar map arguments
+  long long is[kMapMaxScalars];     // integer scalar map arguments
+  long long kidx;                   // mapped_kernel_index() of a multi-kernel convolution
+  int* status;                      // set to 1 by an index outside its buffer (filled by the launcher)
 };
 
-// element access helpers for generated hooks
-template <class T>
-__device__ __forceinline__ T map_ld(const void* p, long long i) {
-  return reinterpret_cast<const T*>(p)[i];
+// Element access of generated hooks, bounds-checked: a map's index
+// expression is user code, so an index outside [0, count) of its buffer
+// loads zero, skips the store and records the fault in the plan's status
+// word instead of touching memory outside the buffer.
+__device__ __forceinline__ bool map_in(const MapArgs& m, int slot, long long i) {
+  if ((unsigned long long)i < (unsigned long long)m.count[slot]) return true;
+  if (m.status) atomicOr(m.status, 1);
+  return false;
 }
 template <class T>
-__device__ __forceinline__ void map_st(void* p, long long i, T v) {
-  reinterpret_cast<T*>(p)[i] = v;
+__device__ __forceinline__ T map_ld(const MapArgs& m, int slot, long long i) {
+  return map_in(m, slot, i) ? reinterpret_cast<const T*>(m.buf[slot])[i] : T(0);
+}
+template <class T>
+__device__ __forceinline__ void map_st(const MapArgs& m, int slot, long long i, T v) {
+  if (map_in(m, slot, i)) reinterpret_cast<T*>(m.buf[slot])[i] = v;
 }
 template <class S, class Re>
-__device__ __forceinline__ Cx<Re> map_ldc(const void* p, long long i) {
-  return Conv<S, Re>::ld(reinterpret_cast<const S*>(p) + i);
+__device__ __forceinline__ Cx<Re> map_ldc(const MapArgs& m, int slot, long long i) {
+  if (!map_in(m, slot, i)) return mk<Re>(Re(0), Re(0));
+  return Conv<S, Re>::ld(reinterpret_cast<const S*>(m.buf[slot]) + i);
 }
 template <class S, class Re>
-__device__ __forceinline__ void map_stc(void* p, long long i, Cx<Re> v) {
-  Conv<S, Re>::st(reinterpret_cast<S*>(p) + i, v);
+__device__ __forceinline__ void map_stc(const MapArgs& m, int slot, long long i, Cx<Re> v) {
+  if (map_in(m, slot, i)) Conv<S, Re>::st(reinterpret_cast<S*>(m.buf[slot]) + i, v);
 }
 
 // Operations of generated hooks, with the reference's shader semantics:

@@ -14,6 +14,7 @@
 #include <nvrtc.h>
 #include <unistd.h>
 
+#include <cstddef>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -27,7 +28,7 @@
 #include "vdx.h"
 #include "vdx_internal.h"
 
-static_assert(sizeof(vdx_map_args) == sizeof(vdx::MapArgs), "vdx_map_args must mirror vdx::MapArgs");
+static_assert(offsetof(vdx::MapArgs, status) == sizeof(vdx_map_args), "vdx::MapArgs must extend vdx_map_args");
 static_assert(VDX_MAP_MAX_BUFFERS == vdx::kMapMaxBuffers && VDX_MAP_MAX_SCALARS == vdx::kMapMaxScalars,
               "map argument limits");
 
@@ -173,6 +174,10 @@ struct vdx_map_plan {
   MapGeometry g;
   Module mod;
   std::string source;
+  int* d_status = nullptr;  // out-of-range map index flag
+  ~vdx_map_plan() {
+    if (d_status) cudaFree(d_status);
+  }
 };
 
 extern "C" {
@@ -210,6 +215,12 @@ int vdx_map_plan_create(const vdx_fft_desc* desc, const char* hooks_source, vdx_
     delete p;
     return rc;
   }
+  cudaError_t se = cudaMalloc(&p->d_status, sizeof(int));
+  if (se == cudaSuccess) se = cudaMemset(p->d_status, 0, sizeof(int));
+  if (se != cudaSuccess) {
+    delete p;
+    return set_error(VDX_ERR_CUDA, (std::string("map plan status word: ") + cudaGetErrorString(se)).c_str());
+  }
   if (g.launch.smem > 48 * 1024) {
     cudaError_t e = cudaKernelSetAttributeForDevice(p->mod.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                     (int)g.launch.smem, g.dev);
@@ -232,14 +243,27 @@ int vdx_map_exec(const vdx_map_plan* p, const vdx_map_args* args, void* stream) 
   int dev = -1;
   cudaGetDevice(&dev);
   if (dev != p->g.dev) return set_error(VDX_ERR_INVALID, "map plan was created on another device");
+  for (int i = 0; i < VDX_MAP_MAX_BUFFERS; ++i)
+    if (args->counts[i] < 0) return set_error(VDX_ERR_INVALID, "map buffer counts must be >= 0");
   FftArgs a = p->g.args;
   MapArgs m;
-  std::memcpy(&m, args, sizeof(m));
+  std::memcpy(&m, args, sizeof(vdx_map_args));
+  m.status = p->d_status;
   void* kargs[] = {&a, &m};
   const Launch& l = p->g.launch;
   cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(p->mod.kernel), l.grid, l.block, kargs, l.smem,
                                    reinterpret_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return set_error(VDX_ERR_CUDA, (std::string("map kernel launch: ") + cudaGetErrorString(e)).c_str());
+  return VDX_OK;
+}
+
+int vdx_map_plan_status(const vdx_map_plan* p, int* status, int reset) {
+  if (!p || !status) return set_error(VDX_ERR_INVALID, "plan and status must be non-NULL");
+  int h = 0;
+  cudaError_t e = cudaMemcpy(&h, p->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && reset) e = cudaMemset(p->d_status, 0, sizeof(int));
+  if (e != cudaSuccess) return set_error(VDX_ERR_CUDA, cudaGetErrorString(e));
+  *status = h;
   return VDX_OK;
 }
 

@@ -225,7 +225,9 @@ struct vdx_plan {
   void* bs_w = nullptr;
   void* bs_K = nullptr;
   void* bs_ws = nullptr;
-  vdx_plan* bs_conv = nullptr;
+  vdx_plan* bs_conv = nullptr;  // fused convolution (M fits one CTA), else:
+  vdx_plan* bs_fwd = nullptr;   // four-step forward transform of length M
+  vdx_plan* bs_inv = nullptr;   // and its normalised inverse
   // one-launch convolve2DR (fft_conv2d.cu)
   int c2_H = 0, c2_W = 0;
   long long c2_images = 0;
@@ -237,6 +239,8 @@ struct vdx_plan {
     if (bs_K) cudaFree(bs_K);
     if (bs_ws) cudaFree(bs_ws);
     delete bs_conv;
+    delete bs_fwd;
+    delete bs_inv;
   }
 };
 
@@ -559,10 +563,13 @@ int plan_bluestein(const vdx_fft_desc& d, long long inner, long long outer, int 
                    vdx_plan** plan) {
   int M = 1;
   while (M < 2 * N - 1) M <<= 1;
-  const int mmax = f64 ? 8192 : 16384;
+  // fp32: up to 2^24 (longer than one CTA: four-step transforms); fp64: the
+  // single-CTA convolution only
+  const int mmax = f64 ? 8192 : (1 << 24);
   if (M > mmax)
     return fail(VDX_ERR_UNSUPPORTED, "Bluestein length " + std::to_string(N) + " needs a " + std::to_string(M) +
                                          "-point convolution (limit " + std::to_string(mmax) + ")");
+  const bool split = M > 16384;
   auto* p = new vdx_plan();
   p->d = d;
   p->op = d.inverse ? OP_C2C_INV : OP_C2C_FWD;
@@ -592,7 +599,19 @@ int plan_bluestein(const vdx_fft_desc& d, long long inner, long long outer, int 
   dc.signal_lo = dc.signal_hi = -1;
   dc.kernel_op = VDX_KOP_MUL_CONJ;
   dc.kernel_broadcast = 1;
-  int rc = create_plan(&dc, Tune{}, &p->bs_conv);
+  int rc = VDX_OK;
+  if (!split) {
+    rc = create_plan(&dc, Tune{}, &p->bs_conv);
+  } else {
+    dc.kind = VDX_KIND_C2C;
+    dc.normalize = 0;
+    rc = create_plan(&dc, Tune{}, &p->bs_fwd);
+    if (rc == VDX_OK) {
+      dc.inverse = 1;
+      dc.normalize = 1;
+      rc = create_plan(&dc, Tune{}, &p->bs_inv);
+    }
+  }
   if (rc != VDX_OK) {
     delete p;
     return rc;
@@ -1288,8 +1307,17 @@ int exec_plan(const vdx_plan* p, const void* in, void* out, const void* kernel, 
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     e = launch_bluestein_io(true, p->store, in, p->bs_ws, p->bs_w, p->outer, p->N, p->bs_M, p->inner, 1.0, s);
     if (e != cudaSuccess) return cuda_fail(e, "Bluestein chirp-in launch");
-    const int rc = exec_plan(p->bs_conv, p->bs_ws, p->bs_ws, p->bs_K, nullptr, stream);
-    if (rc != VDX_OK) return rc;
+    if (p->bs_conv) {
+      const int rc = exec_plan(p->bs_conv, p->bs_ws, p->bs_ws, p->bs_K, nullptr, stream);
+      if (rc != VDX_OK) return rc;
+    } else {
+      int rc = exec_plan(p->bs_fwd, p->bs_ws, p->bs_ws, nullptr, nullptr, stream);
+      if (rc != VDX_OK) return rc;
+      e = launch_bluestein_mul(p->bs_ws, p->bs_K, p->outer, p->bs_M, p->inner, p->f64, s);
+      if (e != cudaSuccess) return cuda_fail(e, "Bluestein spectrum product launch");
+      rc = exec_plan(p->bs_inv, p->bs_ws, p->bs_ws, nullptr, nullptr, stream);
+      if (rc != VDX_OK) return rc;
+    }
     e = launch_bluestein_io(false, p->store, out, p->bs_ws, p->bs_w, p->outer, p->N, p->bs_M, p->inner,
                             norm_scale(p->d.normalize, p->N), s);
     if (e != cudaSuccess) return cuda_fail(e, "Bluestein chirp-out launch");

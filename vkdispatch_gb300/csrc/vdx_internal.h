@@ -105,6 +105,8 @@ struct Conv2dArgs {
 // (cropped, scaled) element-wise launches.
 cudaError_t launch_chirp_tables(void* w, void* b, int N, int M, int sign, bool f64, cudaStream_t s);
 cudaError_t launch_conj_slab(void* K, const void* B, int M, long long inner, bool f64, cudaStream_t s);
+cudaError_t launch_bluestein_mul(void* ws, const void* K, long long outer, int M, long long inner, bool f64,
+                                 cudaStream_t s);
 cudaError_t launch_bluestein_io(bool in_phase, int store, const void* x, void* ws, const void* w, long long outer,
                                 int N, int M, long long inner, double scale, cudaStream_t s);
 

@@ -168,6 +168,22 @@ def _staged(plan_fn, out_buf, out_kind, in_buf, in_kind, shape, compute, graph, 
     _record(graph, launch, (in_buf, out_buf, stage_in, stage_out) + tuple(keep))
 
 
+def _strided(*groups) -> bool:
+    """Whether any Buffer among the arguments addresses a non-contiguous array."""
+    return any(isinstance(b, Buffer) and not b.contiguous for g in groups for b in (g or ()))
+
+
+def _check_strided_defaults(shape, slab, bufs, kernel) -> None:
+    """A non-contiguous buffer read or written without a map is addressed by
+    the transform's own io_index, so it must have the transform's shape (a
+    broadcast kernel: the shape of one slab)."""
+    for b in bufs:
+        if isinstance(b, Buffer) and not b.contiguous and tuple(b.shape) != tuple(shape):
+            raise ValueError(f"a non-contiguous buffer of shape {b.shape} needs buffer_shape == its shape")
+    if isinstance(kernel, Buffer) and not kernel.contiguous and kernel.size not in (math.prod(shape), slab):
+        raise ValueError(f"a non-contiguous kernel of shape {kernel.shape} must hold one slab or the whole signal")
+
+
 def _signal(sr, N: int) -> Optional[Tuple[int, int]]:
     if sr is None:
         return None
@@ -213,6 +229,8 @@ def fft(
             raise ValueError("output_type cannot be provided when output_map is used")
         outs, ins, _ = _split_buffers(buffers, input_map, output_map)
         try:
+            if _strided(outs, ins):
+                raise NotImplementedError("non-contiguous buffers")
             out_buf, out_kind, in_buf, in_kind = _io_ends(outs, ins, input_map, output_map)
         except NotImplementedError as menu:
             _jit_transform(outs, ins, [], input_map, output_map, None, False, buffer_shape, axis, inverse,
@@ -233,6 +251,13 @@ def fft(
                 out_buf, out_kind, in_buf, in_kind, shape, compute, graph)
         return
     buf = buffers[0]
+    if not buf.contiguous:
+        if r2c:
+            raise ValueError("R2C/C2R transforms need a contiguous buffer")
+        _jit_transform([buf], [], [], None, None, None, False, buffer_shape, axis, inverse,
+                       bool(inverse and normalize_inverse), compute_type, input_signal_range, graph, print_shader,
+                       "non-contiguous buffer")
+        return
     memo_key = (buf.var_type, buf.shape, buf.size, None if buffer_shape is None else tuple(buffer_shape), axis,
                 bool(inverse), bool(normalize_inverse), bool(r2c), output_type, input_type, compute_type,
                 None if input_signal_range is None else tuple(input_signal_range))
@@ -419,6 +444,11 @@ def convolve(
                          output_map, compute_type, input_signal_range)
         return
     buf, ker = buffers[0], buffers[1]
+    if _strided([buf, ker]):
+        _jit_transform([buf], [], [ker], None, None, None, True, buffer_shape, axis, False, bool(normalize),
+                       compute_type, input_signal_range, graph, print_shader, "non-contiguous buffer",
+                       kernel_inner_only=kernel_inner_only)
+        return
     if buffer_shape is None:
         buffer_shape = buf.shape
     buffer_shape = tuple(int(s) for s in buffer_shape)
@@ -468,6 +498,8 @@ def _convolve_mapped(buffers, kernel_map, buffer_shape, graph, axis, normalize, 
 
     outs, ins, kers = _split_buffers(buffers, input_map, output_map, kernel_map, conv=True)
     try:
+        if _strided(outs, ins, kers):
+            raise NotImplementedError("non-contiguous buffers")
         out_buf, out_kind, in_buf, in_kind = _io_ends(outs, ins, input_map, output_map)
         km = M.classify_kernel(kernel_map) if kernel_map is not None else M.KernelMap("conj_mul", 0,
                                                                                      kers[0].var_type)
@@ -548,6 +580,8 @@ def _convolve_multi(buffers, kernel_map, kernel_num, buffer_shape, graph, axis, 
 
     outs, ins, kers = _split_buffers(buffers, input_map, output_map, kernel_map, conv=True)
     try:
+        if _strided(outs, ins, kers):
+            raise NotImplementedError("non-contiguous buffers")
         _classify_multi(input_map, output_map, kernel_map)
     except NotImplementedError as menu:
         _jit_transform(outs, ins, kers, input_map, output_map, kernel_map, True, buffer_shape, axis, False,
@@ -665,6 +699,9 @@ def _jit_transform(outs, ins, kers, input_map, output_map, kernel_map, conv, buf
     shape = tuple(int(x) for x in (buffer_shape if buffer_shape is not None else first.shape))
     ax = _norm_axis(axis, len(shape))
     total, slab = math.prod(shape), math.prod(shape[ax:])
+    _check_strided_defaults(shape, slab,
+                            ([outs[0]] if output_map is None else []) + ([(ins or outs)[0]] if input_map is None else []),
+                            kers[0] if conv and kernel_map is None else None)
     bslab = 0
     if conv and kernel_map is None:
         kb = kers[0]

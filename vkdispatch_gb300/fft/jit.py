@@ -10,6 +10,10 @@ with NVRTC into its own FFT kernel template (vdx_map_plan_create, csrc/
 fft_mapped.cuh).  The FFT passes stay hand-written; only the element I/O and
 the spectrum operation are user code.
 
+Buffers over non-contiguous arrays (from_cuda_array with
+require_contiguous=False) run through the same hooks: every index into
+them, default or user-written, becomes the sum of coordinate * stride.
+
 Supported inside maps: buffer loads and stores at any integer index
 expression (io_index, fft_index, fft_size, mapped_kernel_index(), integer
 arithmetic, vc.ravel_index / vc.unravel_index), scalar map arguments
@@ -47,6 +51,26 @@ _STORAGE = {
 
 _UNARY = {"sin", "cos", "tan", "asin", "acos", "atan", "sinh", "cosh", "tanh", "exp", "exp2", "log", "log2", "sqrt",
           "inversesqrt", "abs", "floor", "ceil", "trunc", "round", "fract", "sign"}
+
+
+def phys_index(buf, ix: str) -> str:
+    """The element offset of flat index ix (in the buffer's shape) of a
+    buffer: ix itself in C order, else the sum of coordinate * stride."""
+    strides = getattr(buf, "strides", None)
+    if strides is None:
+        return ix
+    shape = tuple(int(d) for d in buf.shape)
+    terms = []
+    for i, (d, st) in enumerate(zip(shape, strides)):
+        inner = 1
+        for x in shape[i + 1:]:
+            inner *= x
+        c = f"(({ix}) / {inner}LL)" if inner > 1 else f"({ix})"
+        if i > 0 and d > 1:
+            c = f"({c} % {d}LL)"
+        if d > 1 and st:
+            terms.append(f"{c} * {st}LL")
+    return "(" + (" + ".join(terms) or "0LL") + ")"
 
 
 def _wider(*kinds: str) -> str:
@@ -87,6 +111,7 @@ class _Lower:
         self.name = name
         self.types = types
         self.bind: Dict[int, Tuple[str, int]] = {}
+        self.objs: Dict[int, object] = {}
         self.regs: Dict[str, str] = {"reg": "c"}
         for i, (t, sc, a) in enumerate(zip(types, scalar_flags, args)):
             if sc:
@@ -97,6 +122,7 @@ class _Lower:
                 if getattr(a, "var_type", None) is not None and a.var_type != t:
                     raise ValueError(f"map {name}: buffer of type {a.var_type.name} passed for a {t.name} argument")
                 self.bind[i] = ("b", slots.add_buffer(a))
+                self.objs[i] = a
 
     def fail(self, what):
         raise NotImplementedError(f"map {self.name}: {what} is not supported by the map-hook compiler")
@@ -262,34 +288,34 @@ class _Lower:
 
     def load(self, i, idx) -> Tuple[str, str]:
         slot, (ctype, kind) = self.buffer(i)
-        ix = self.index(idx)
+        ix = phys_index(self.objs[i], self.index(idx))
         if kind == "c":
             return self.ldc(ctype, slot, ix), "c"
         if kind == "f":
-            return f"vdx::map_ld<{ctype}>(m.buf[{slot}], {ix})", "f"
-        return f"(long long)vdx::map_ld<{ctype}>(m.buf[{slot}], {ix})", "i"
+            return f"vdx::map_ld<{ctype}>(m, {slot}, {ix})", "f"
+        return f"(long long)vdx::map_ld<{ctype}>(m, {slot}, {ix})", "i"
 
     @staticmethod
     def ldc(ctype, slot, ix) -> str:
         if ctype == "vdx::c32s":  # complex32 converts through float
-            return f"vdx::mapops::to_cx<Re>(vdx::map_ldc<vdx::c32s, float>(m.buf[{slot}], {ix}))"
-        return f"vdx::map_ldc<{ctype}, Re>(m.buf[{slot}], {ix})"
+            return f"vdx::mapops::to_cx<Re>(vdx::map_ldc<vdx::c32s, float>(m, {slot}, {ix}))"
+        return f"vdx::map_ldc<{ctype}, Re>(m, {slot}, {ix})"
 
     @staticmethod
     def stc(ctype, slot, ix, val) -> str:
         if ctype == "vdx::c32s":
-            return f"vdx::map_stc<vdx::c32s, float>(m.buf[{slot}], {ix}, vdx::mapops::to_cx<float>({val}));"
-        return f"vdx::map_stc<{ctype}, Re>(m.buf[{slot}], {ix}, {val});"
+            return f"vdx::map_stc<vdx::c32s, float>(m, {slot}, {ix}, vdx::mapops::to_cx<float>({val}));"
+        return f"vdx::map_stc<{ctype}, Re>(m, {slot}, {ix}, {val});"
 
     def store(self, i, idx, value) -> str:
         slot, (ctype, kind) = self.buffer(i)
-        ix = self.index(idx)
+        ix = phys_index(self.objs[i], self.index(idx))
         c, k = self.expr(value)
         if kind == "c":
             return self.stc(ctype, slot, ix, self.as_kind(c, k, "c"))
         if k == "c":
             self.fail("a complex value stored to a real buffer")
-        return f"vdx::map_st<{ctype}>(m.buf[{slot}], {ix}, ({ctype})({c}));"
+        return f"vdx::map_st<{ctype}>(m, {slot}, {ix}, ({ctype})({c}));"
 
     # ---- statements
     def statements(self, events) -> List[str]:
@@ -385,7 +411,7 @@ def build_hooks(outs, ins, kers, input_map, output_map, kernel_map, conv: bool, 
         body.append("(void)reg;")
     else:
         slot, ctype = complex_buffer(outs[0], "output")
-        body = [_Lower.stc(ctype, slot, "io", "v")]
+        body = [_Lower.stc(ctype, slot, phys_index(outs[0], "io"), "v")]
     store = _hook("void store(const vdx::MapArgs& m, vdx::Cx<Re> v, long long io, int k, int n)",
                   body + ["(void)k; (void)n; (void)m;"])
     # load (input map)
@@ -395,7 +421,7 @@ def build_hooks(outs, ins, kers, input_map, output_map, kernel_map, conv: bool, 
     else:
         src = ins[0] if ins else outs[0]
         slot, ctype = complex_buffer(src, "input")
-        body = [f"return {_Lower.ldc(ctype, slot, 'io')};"]
+        body = [f"return {_Lower.ldc(ctype, slot, phys_index(src, 'io'))};"]
     load = _hook("vdx::Cx<Re> load(const vdx::MapArgs& m, long long io, int k, int n)",
                  ["(void)k; (void)n; (void)m;"] + body)
     # kernel (kernel map), convolutions only
@@ -407,7 +433,7 @@ def build_hooks(outs, ins, kers, input_map, output_map, kernel_map, conv: bool, 
     else:
         slot, ctype = complex_buffer(kers[0] if kers else None, "kernel")
         kio = f"(io % {kernel_broadcast_slab}LL)" if kernel_broadcast_slab else "io"
-        body = [f"return vdx::cmulc(v, {_Lower.ldc(ctype, slot, kio)});"]
+        body = [f"return vdx::cmulc(v, {_Lower.ldc(ctype, slot, phys_index(kers[0], kio))});"]
     kernel = _hook("vdx::Cx<Re> kernel(const vdx::MapArgs& m, vdx::Cx<Re> v, long long io, int k, int n)",
                    ["(void)k; (void)n; (void)m; (void)io;"] + body)
     src = "struct VdxHooks {\n" + load + store + kernel + "};\n"
@@ -434,12 +460,28 @@ class MapPlan:
     def exec(self, args, stream) -> None:
         L.check(L.lib().vdx_map_exec(self.handle, ctypes.byref(args), stream), "map exec")
 
+    def status(self, reset: bool = False) -> int:
+        """1 when a launch of this plan indexed a map buffer out of range
+        (synchronous); reset clears it."""
+        st = ctypes.c_int()
+        L.check(L.lib().vdx_map_plan_status(self.handle, ctypes.byref(st), int(reset)), "map status")
+        return int(st.value)
+
     def __del__(self):
         try:
             if self.handle:
                 L.lib().vdx_map_plan_destroy(self.handle)
         except Exception:
             pass
+
+
+def out_of_range(reset: bool = True) -> bool:
+    """Whether any compiled map plan of the current device indexed a map
+    buffer outside its extent since the last reset (synchronous)."""
+    import torch
+
+    dev = torch.cuda.current_device()
+    return any(p.status(reset) for k, p in list(_plans.items()) if k[0] == dev)
 
 
 def get_plan(shape, axis, conv, inverse, normalize, code, sig, source) -> MapPlan:
@@ -464,10 +506,20 @@ def get_plan(shape, axis, conv, inverse, normalize, code, sig, source) -> MapPla
     return p
 
 
+def extent(buf) -> int:
+    """Elements a buffer may be indexed with: its size in C order, else one
+    past its largest strided offset."""
+    strides = getattr(buf, "strides", None)
+    if strides is None:
+        return int(buf.size)
+    return 1 + sum((int(d) - 1) * int(s) for d, s in zip(buf.shape, strides))
+
+
 def make_args(slots: Slots, kernel_index: int = 0):
     a = L.MapArgs()
     for i, b in enumerate(slots.buffers):
         a.buffers[i] = b.ptr
+        a.counts[i] = extent(b)
     for i, v in enumerate(slots.fscalars):
         a.fscalars[i] = v
     for i, v in enumerate(slots.iscalars):

@@ -37,12 +37,20 @@ def autotune(enabled: bool = True):
         _tls.tune = old
 
 
+def bluestein_enabled() -> bool:
+    """Whether C2C axes with a prime factor above 13 plan as Bluestein
+    transforms on this thread (the default)."""
+    return getattr(_tls, "bluestein", True)
+
+
 @contextlib.contextmanager
 def bluestein(enabled: bool = True):
-    """Within the block, C2C axes whose length has a prime factor above 13
-    (which the reference rejects) are planned as Bluestein chirp-z
-    transforms instead of raising.  Per thread."""
-    old = getattr(_tls, "bluestein", False)
+    """C2C axes whose length has a prime factor above 13 (which the
+    reference's planner rejects, vkdispatch/fft/prime_utils.py:6-10) are
+    planned as Bluestein chirp-z transforms by default; ``with
+    vd.fft.bluestein(False):`` restores the reference's ValueError for such
+    lengths inside the block.  Per thread."""
+    old = bluestein_enabled()
     _tls.bluestein = bool(enabled)
     try:
         yield
@@ -150,7 +158,7 @@ def get_plan(
             flags = L.VDX_FFT_FLAG_TENSOR_CORE
         if getattr(_tls, "tune", False):
             flags |= L.VDX_FFT_FLAG_AUTOTUNE
-        if getattr(_tls, "bluestein", False) and kind == L.VDX_KIND_C2C:
+        if bluestein_enabled() and kind == L.VDX_KIND_C2C:
             flags |= L.VDX_FFT_FLAG_BLUESTEIN
     key = (dev, tuple(shape), axis, kind, bool(inverse), int(normalize), io_type, compute_type, signal_range,
            kernel_op, kernel_type, bool(kernel_broadcast), int(flags))

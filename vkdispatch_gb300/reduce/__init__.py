@@ -202,6 +202,20 @@ class ReduceFunction:
         in_code = src.var_type.vdx_code
         ptr, out = src.ptr, res.ptr
         ws = out + batch * out_type.item_size
+        if not src.contiguous:
+            # a non-contiguous array is reduced from a C-order copy made in the launch
+            import torch
+
+            tmp = torch.empty(src.tensor.shape, dtype=src.tensor.dtype, device=src.tensor.device)
+            ptr = tmp.data_ptr()
+
+            def launch(stream):
+                with torch.cuda.stream(torch.cuda.ExternalStream(stream) if stream else torch.cuda.current_stream()):
+                    tmp.copy_(src.tensor, non_blocking=True)
+                L.check(L.lib().vdx_reduce(op, map_code, in_code, ptr, n, batch, out, ws, stream), "reduce")
+
+            G.resolve(graph).record(launch, (src, res, tmp))
+            return res
 
         def launch(stream):
             L.check(L.lib().vdx_reduce(op, map_code, in_code, ptr, n, batch, out, ws, stream), "reduce")
