@@ -92,7 +92,7 @@ def test_strided_axes_and_chunks(shape, axis, ws_mb):
     rng = np.random.default_rng(sum(shape) + (ws_mb or 7))
     x = crandn(rng, shape)
     t = torch.from_numpy(x).cuda()
-    p = _plan(shape, axis, VDX_FOURSTEP_WS_MB=ws_mb)
+    p = _plan(shape, axis, VDX_FOURSTEP_WS_MB=ws_mb, VDX_FOURSTEP_FUSED=None if ws_mb is None else 0)
     assert p.describe()["strided"] is True
     _run(p, t)
     ref = np.fft.fft(x.astype(np.complex128), axis=axis)
@@ -104,7 +104,8 @@ def test_contiguous_chunks(ws_mb):
     rng = np.random.default_rng(5)
     x = crandn(rng, (20, 16384))
     t = torch.from_numpy(x).cuda()
-    p = _plan((20, 16384), 1, VDX_FOURSTEP_WS_MB=ws_mb)
+    # workspace chunks belong to the two-launch form
+    p = _plan((20, 16384), 1, VDX_FOURSTEP_WS_MB=ws_mb, VDX_FOURSTEP_FUSED=0)
     d = p.describe()
     assert d["chunk_outer"] == (8 if ws_mb == 1 else 20)
     _run(p, t)
@@ -174,3 +175,48 @@ def test_half_storage_strided_tiles(vt, shape, axis, ws_mb):
     tol = 5e-3 if vt == vd.complexbf16 else 1.2e-3
     assert rel_l2(got, np.fft.fft(q, axis=axis)) < tol
     P.cache_clear()
+
+
+@pytest.mark.parametrize("shape,axis", [((16384, 40), 0), ((2, 16384, 37), 1), ((5, 16384), 1), ((4096, 70), 0),
+                                        ((9, 4096), 1), ((3, 65536), 1), ((65536, 3), 0)])
+@pytest.mark.parametrize("inverse", [False, True])
+def test_fused_four_step_matches_numpy_and_two_launch_form(shape, axis, inverse):
+    """The opt-in fused form (VDX_FOURSTEP_FUSED=1: both passes of a square
+    split in one persistent launch with an L2-resident ring, csrc/
+    fft_fused4.cu) against FP64 numpy and against the default two-launch
+    form, out of place."""
+    rng = np.random.default_rng(sum(shape) + axis + inverse)
+    x = crandn(rng, shape)
+    src = torch.from_numpy(x).cuda()
+    # VDX_FOURSTEP_MIN=1: four-step for the 4096-point axes too (64 x 64 splits)
+    fused = _plan(shape, axis, inverse=inverse, normalize=inverse, VDX_FOURSTEP_MIN=1, VDX_FOURSTEP_FUSED=1)
+    plain = _plan(shape, axis, inverse=inverse, normalize=inverse, VDX_FOURSTEP_MIN=1, VDX_FOURSTEP_FUSED=0)
+    assert fused.describe()["fused"] and not plain.describe()["fused"]
+    outs = []
+    for p in (fused, plain):
+        out = torch.empty_like(src)
+        p.exec(src.data_ptr(), out.data_ptr(), None, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        outs.append(out.cpu().numpy())
+    assert fused.status() == 0
+    x64 = x.astype(np.complex128)
+    ref = np.fft.ifft(x64, axis=axis) if inverse else np.fft.fft(x64, axis=axis)
+    n = shape[axis]
+    assert rel_l2(outs[0], ref) <= tol_fp32(n)
+    assert rel_l2(outs[0], outs[1]) <= tol_fp32(n)
+
+
+@pytest.mark.parametrize("vt,tol", [(vd.complexbf16, 5e-3), (vd.complex32, 1.2e-3)])
+@pytest.mark.parametrize("shape,axis", [((16384, 48), 0), ((3, 16384), 1)])
+def test_fused_four_step_half_storage(vt, tol, shape, axis):
+    rng = np.random.default_rng(77 + axis)
+    x = crandn(rng, shape) * 0.25
+    buf = vd.Buffer(shape, vt)
+    buf.write(x)
+    q = buf.read(0).astype(np.complex128)
+    io = L.VDX_BF16X2 if vt == vd.complexbf16 else L.VDX_C32
+    p = _plan(shape, axis, io=io, VDX_FOURSTEP_FUSED=1)
+    assert p.describe()["fused"]
+    _run(p, buf.tensor)
+    assert p.status() == 0
+    assert rel_l2(buf.read(0), np.fft.fft(q, axis=axis)) < tol

@@ -210,6 +210,11 @@ struct vdx_plan {
   size_t smemA = 0, smemB = 0;
   void* ws = nullptr;
   size_t ws_bytes = 0;
+  // both passes in one persistent launch with an L2-resident ring (fft_fused4.cu)
+  bool fused = false;
+  FusedLaunch fl{};
+  unsigned* d_ticket = nullptr;
+  int* d_done = nullptr;  // 2 R counters
   // tensor-core short transforms (VDX_FFT_FLAG_TENSOR_CORE)
   bool tensor_core = false;
   const void* tc_bmat = nullptr;  // DFT operand image, shared per (device, direction)
@@ -235,6 +240,8 @@ struct vdx_plan {
   ~vdx_plan() {
     if (ws) cudaFree(ws);
     if (d_status) cudaFree(d_status);
+    if (d_ticket) cudaFree(d_ticket);
+    if (d_done) cudaFree(d_done);
     if (bs_w) cudaFree(bs_w);
     if (bs_K) cudaFree(bs_K);
     if (bs_ws) cudaFree(bs_ws);
@@ -263,6 +270,98 @@ int sub_pass_plan(int n, int M, PassPlan& pp, std::string& why) {
   pp.M = M;
   pp.npad = n + 1 + ((n + 1) >> 4) + 1;
   set_pass_tables(pp);
+  return VDX_OK;
+}
+
+// The fused form of a square four-step split (fft_fused4.cu): tile width,
+// persistent grid from the kernel's occupancy, queue lag L and ring of
+// R = L + 1 group slots sized so that the ring stays far below L2.
+int plan_fused_fourstep(vdx_plan* p, int N1, int N0, long long inner, long long outer, PassPlan pp, size_t sb) {
+  const int N = p->N;
+  const bool strided = inner > 1;
+  int M = strided ? 32 : 16;
+  if (const char* e = std::getenv("VDX_FUSED_COLUMNS")) M = std::max(8, std::min(32, std::atoi(e)));
+  if (strided) M = (int)std::min<long long>(M, inner);
+  M = std::max(1, std::min(M, 256 / pp.T));
+  pp.M = M;
+  pp.mmag = inv_magic(M);
+  const size_t smem = size_t(N1 + 1) * M * 8;
+  int per_sm = 0;
+  cudaError_t e = fused_fourstep_ctas_per_sm(p->store, pp, smem, &per_sm);
+  if (e != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    return fail(VDX_ERR_UNSUPPORTED, "no fused four-step kernel for this split");
+  }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->dev);
+  const long long grid = (long long)per_sm * std::max(1, sms);
+  const long long nA = strided ? N0 : (N0 + M - 1) / M, nB = strided ? N1 : (N1 + M - 1) / M;
+  const long long slot = strided ? (long long)N * M : (long long)N;
+  const long long slot_bytes = slot * (long long)sb;
+  // span = queue stages the resident CTAs cover at once.  Pass B of group g
+  // is queued L = 2 spans after its pass A, so its inputs are done when it
+  // runs; a ring slot is reused R = L + span + 2 groups later, so the pass B
+  // that last read it has finished too (with R = L + 1 the reuse wait falls
+  // inside the window of running units and stalls most pass-A units).
+  const long long span = std::max(1ll, (grid + nA + nB - 1) / (nA + nB));
+  long long L = 2 * span;
+  if (const char* e2 = std::getenv("VDX_FUSED_LAG")) L = std::max(1ll, std::atoll(e2));
+  long long extra = span + 2;
+  const long long ring_cap = 64ll << 20;  // half the 126 MB L2
+  while (L > 1 && (L + extra) * slot_bytes > ring_cap) {
+    --L;
+    if (extra > 2 && (L + extra) * slot_bytes > ring_cap) --extra;
+  }
+  const long long groups = strided ? outer * ((inner + M - 1) / M) : outer;
+  L = std::min(L, std::max(1ll, groups));
+  const int R = int(L + extra);
+  p->fused = true;
+  p->fourstep = true;
+  p->N1 = N1;
+  p->N0 = N0;
+  p->inner = inner;
+  p->outer = outer;
+  p->ws_bytes = size_t(R) * size_t(slot_bytes);
+  FusedLaunch& fl = p->fl;
+  fl.ppA = fl.ppB = pp;
+  fl.N = N;
+  fl.N0 = N0;
+  fl.N1 = N1;
+  fl.inner = inner;
+  fl.outer = outer;
+  fl.M = M;
+  fl.scale = float(p->args.scale);
+  fl.L = int(L);
+  fl.R = R;
+  fl.store = p->store;
+  fl.inverse = p->op == OP_C2C_INV;
+  fl.strided = strided;
+  fl.grid = (unsigned)grid;
+  fl.smem = smem;
+  int rc = get_table(p->dev, N1, N1, false, const_cast<void**>(&fl.twA));
+  if (rc == VDX_OK) rc = get_table(p->dev, N0, N0, false, const_cast<void**>(&fl.twB));
+  if (rc == VDX_OK) rc = get_table(p->dev, N, N, false, const_cast<void**>(&fl.twl));
+  if (rc != VDX_OK) return rc;
+  e = cudaMalloc(&p->ws, p->ws_bytes);
+  if (e != cudaSuccess) {
+    p->ws = nullptr;
+    return fail(VDX_ERR_NOMEM, std::string("four-step ring: ") + cudaGetErrorString(e));
+  }
+  e = cudaMalloc(reinterpret_cast<void**>(&p->d_status), sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->d_ticket), sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->d_done), sizeof(int) * 2 * size_t(R));
+  if (e != cudaSuccess) return cuda_fail(e, "fused four-step counters");
+  fl.ring = p->ws;
+  fl.ticket = p->d_ticket;
+  fl.doneA = p->d_done;
+  fl.doneB = p->d_done + R;
+  fl.status = p->d_status;
+  p->fsA.pp = p->fsB.pp = pp;
+  p->blockA = p->blockB = dim3(pp.T * M);
+  p->smemA = p->smemB = smem;
+  p->chunk_cols = inner;
+  p->chunk_outer = outer;
   return VDX_OK;
 }
 
@@ -309,6 +408,23 @@ int plan_fourstep(vdx_plan* p, long long inner, long long outer, int smem_optin)
   ppB.mmag = inv_magic(ppB.M);
   if (ppA.T * ppA.M > 512 || ppB.T * ppB.M > 512)
     return fail(VDX_ERR_UNSUPPORTED, "four-step sub-transform needs more than 512 threads");
+
+  // Square splits (the same compile-time short plan for both passes) can run
+  // as one persistent launch whose intermediate stays in an L2-resident ring
+  // (fft_fused4.cu) with VDX_FOURSTEP_FUSED=1.  It halves the HBM traffic but
+  // measured slower on GB300 (16384^2 complex64: 2.16-2.25 ms per axis
+  // against 1.37-1.56 ms for the two launches, bf16 the same): each unit's
+  // claim, dependency check and load -> compute -> store run in series, and
+  // three to six resident CTAs per SM do not hide that, while the two-launch
+  // passes already move their traffic at about 0.9 of the measured HBM peak.
+  if (!p->tensor_core && N1 == N0 && (p->store == ST_C64 || p->store == ST_C32 || p->store == ST_BF16)) {
+    const char* fe = std::getenv("VDX_FOURSTEP_FUSED");
+    if (fe && std::atoi(fe) == 1) {
+      const int rc = plan_fused_fourstep(p, N1, N0, inner, outer, ppA, sb);
+      if (rc == VDX_OK) return VDX_OK;
+      if (rc != VDX_ERR_UNSUPPORTED) return rc;
+    }
+  }
 
   // workspace bytes per chunk; 0 = the whole array in one pair of launches.
   // Chunks small enough to stay in L2 save HBM traffic but each launch is
@@ -449,6 +565,12 @@ bool fourstep_tma() {
 }
 
 cudaError_t exec_fourstep(const vdx_plan* p, const void* in, void* out, cudaStream_t s) {
+  if (p->fused) {
+    FusedLaunch fl = p->fl;
+    fl.in = in;
+    fl.out = out;
+    return launch_fused_fourstep(fl, s);
+  }
   const long long N = p->N, N0 = p->N0, N1 = p->N1, inner = p->inner, outer = p->outer;
   const size_t sb = store_bytes(p->store);
   const bool inv = p->op == OP_C2C_INV;
@@ -1248,11 +1370,12 @@ int vdx_fft_plan_describe(const vdx_plan* p, char* buf, size_t n) {
                   "{\"op\": \"%s\", \"N\": %d, \"fourstep\": [%d, %d], \"strided\": %s, "
                   "\"columns_per_tile\": [%d, %d], \"chunk_columns\": %lld, \"chunk_outer\": %lld, "
                   "\"workspace_bytes\": %zu, \"block\": [%u, %u], \"smem\": [%zu, %zu], \"tensor_core\": %s, "
-                  "\"autotuned\": %s, \"tune_candidates\": %d}",
+                  "\"autotuned\": %s, \"tune_candidates\": %d, \"fused\": %s, \"ring_slots\": %d, "
+                  "\"grid\": %u}",
                   p->op == OP_C2C_INV ? "c2c_inv" : "c2c_fwd", p->N, p->N1, p->N0, p->inner > 1 ? "true" : "false",
                   p->fsA.pp.M, p->fsB.pp.M, p->chunk_cols, p->chunk_outer, p->ws_bytes, p->blockA.x, p->blockB.x,
                   p->smemA, p->smemB, p->tensor_core ? "true" : "false", p->tuned ? "true" : "false",
-                  p->tuned_candidates);
+                  p->tuned_candidates, p->fused ? "true" : "false", p->fused ? p->fl.R : 0, p->fused ? p->fl.grid : 0);
     return VDX_OK;
   }
   if (p->op == OP_CONV2D_REAL) {

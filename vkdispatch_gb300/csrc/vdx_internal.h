@@ -88,6 +88,34 @@ cudaError_t launch_fourstep_pass_tc(const FsArgs& a, const Launch& l, int store,
 cudaError_t tc_dft_operands(int dev, bool inv, const void** out);
 size_t tc_pass_smem(int mt);
 
+// Both passes of a four-step long axis in one persistent launch with an
+// L2-resident ring for the intermediate (fft_fused4.cu).  Square splits
+// (N0 == N1, the same compile-time short plan for both passes) only.
+struct FusedLaunch {
+  PassPlan ppA, ppB;  // short-transform plans; M = columns per tile, equal for both
+  const void* in;
+  void* out;
+  void* ring;  // R slots: N * M elements each (strided axes) or N (contiguous)
+  const void* twA;
+  const void* twB;
+  const void* twl;
+  long long N, N0, N1, inner, outer;
+  int M;
+  float scale;
+  int L, R;
+  unsigned* ticket;
+  int* doneA;  // R counters each
+  int* doneB;
+  int* status;
+  long long wait_limit;  // 0 = default
+  int store;
+  bool inverse, strided;
+  unsigned grid;
+  size_t smem;
+};
+cudaError_t fused_fourstep_ctas_per_sm(int store, const PassPlan& pp, size_t smem, int* per_sm);
+cudaError_t launch_fused_fourstep(const FusedLaunch& fl, cudaStream_t s);
+
 // One-launch 2-D convolution of real images (fft_conv2d.cu): one image per
 // thread-block cluster, the half spectrum held in the cluster's shared memory.
 struct Conv2dArgs {
