@@ -230,6 +230,13 @@ def _run_ours(args):
     torch.cuda.synchronize()
 
     K = args.steps
+    # Timed region: events around each whole step only.  The three kernels
+    # are launched with programmatic dependent launch, which lets each one be
+    # scheduled while the previous one drains; an event recorded between two
+    # kernels would serialise them, so the per-kernel durations (for the
+    # roofline of the dominant kernel) come from a second pass of the same K
+    # steps with events between the kernels.
+    sev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(K)]
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(K)]
     clocks = ClockSampler(local)
     clocks.start()
@@ -241,20 +248,25 @@ def _run_ours(args):
     torch.cuda.nvtx.range_push("timed")  # lets ncu --nvtx-include "timed/" skip plan creation and autotuning
     for i in range(K):
         flush.zero_()
-        step(evs[i])
+        sev[i][0].record(stream)
+        step()
+        sev[i][1].record(stream)
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
     wall = time.perf_counter() - t0
+    for i in range(K):  # the kernel pass
+        flush.zero_()
+        step(evs[i])
+    torch.cuda.synchronize()
     clk = clocks.stop()
     per = {"r2c": [], "conv": [], "c2r": []}
-    steps_ms = []
+    steps_ms = [e[0].elapsed_time(e[1]) for e in sev]
     for e in evs:
         per["r2c"].append(e[0].elapsed_time(e[1]))
         per["conv"].append(e[1].elapsed_time(e[2]))
         per["c2r"].append(e[2].elapsed_time(e[3]))
-        steps_ms.append(e[0].elapsed_time(e[3]))
     ms = max_over_ranks(statistics.mean(steps_ms), dist)
     value = whole_job_gbps(world, STEP_BYTES, ms)
 
@@ -348,6 +360,7 @@ def _run_ours(args):
                 "parallelism": "replicas" if world > 1 else "single GPU",
                 "error_rel_l2_vs_fp64": err,
                 "per_kernel_ms": {k: round(v, 5) for k, v in mean_k.items()},
+                "kernel_ms_from": "second pass with events between kernels",
                 "wall_s_timed_region": round(wall, 4),
             },
             "roofline": {

@@ -404,6 +404,18 @@ struct IsFixPlan : FalseT {};
 template <int N_, int T_, class L, int MAXE_>
 struct IsFixPlan<FixPlan<N_, T_, L, MAXE_>> : TrueT {};
 
+// Programmatic dependent launch.  These kernels are launched with
+// programmatic stream serialisation (enqueue_pdl): the next kernel of the
+// stream may be scheduled while this one's last CTAs still run, and this one
+// may have been scheduled before the previous kernel finished.  So every CTA
+// first lets its successor launch, then waits until the previous kernel of
+// the stream has completed and its writes are visible -- before any global
+// memory access.  Launched without the attribute, both are no-ops.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 template <class Re>
 __device__ __forceinline__ Cx<Re>* smem_base() {
   extern __shared__ __align__(16) unsigned char vdx_smem_raw[];
@@ -463,6 +475,7 @@ __device__ __forceinline__ void store_output(const Plan& P, const Place<STRIDED>
 // 128 registers per thread.
 template <class Plan, bool INV, bool STRIDED, class S, class Re, int IW = 0, int LOSS = 0>
 __global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 32 ? 2 : 1) k_c2c(FftArgs a) {
+  pdl_enter();
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
   const Place<STRIDED> pl(a, P.T());
@@ -537,6 +550,7 @@ __global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 3
 // (the kernel-spectrum gradient X conj(G) / N of an FFT convolution).
 template <class Plan, bool STRIDED, class S, class K, class Re, int KOP, int SPEC = 0>
 __global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 32 ? 2 : 1) k_conv(FftArgs a) {
+  pdl_enter();
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
   const Place<STRIDED> pl(a, P.T());
@@ -597,6 +611,7 @@ __global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 3
 // forward FFT.  The kernel spectrum is read once, with evict-first loads.
 template <class Plan, class S, class Re, int KOP>
 __global__ void __launch_bounds__(256, Plan::MAXE <= 8 ? 3 : 2) k_conv_pf(FftArgs a) {
+  pdl_enter();
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
   const Place<true> pl(a, P.T());
@@ -657,6 +672,7 @@ __global__ void __launch_bounds__(256, Plan::MAXE <= 8 ? 3 : 2) k_conv_pf(FftArg
 template <class Plan, bool STRIDED, class S, class Re, int KOP>
 __global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 32 ? 2 : 1)
     k_conv_multi(FftArgs a, int K, long long kstride, long long ostride) {
+  pdl_enter();
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
   const Place<STRIDED> pl(a, P.T());
@@ -710,6 +726,7 @@ __global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 3
 // ---------------------------------------------------------------------------
 template <class Plan, class S, class Re>
 __global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 32 ? 2 : 1) k_r2c_even(FftArgs a) {
+  pdl_enter();
   using SR = typename RealOf<S>::type;
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
@@ -777,6 +794,7 @@ __global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 3
 // ---------------------------------------------------------------------------
 template <class Plan, class S, class Re>
 __global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 32 ? 2 : 1) k_c2r_even(FftArgs a) {
+  pdl_enter();
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;
   const Place<false> pl(a, P.T());
@@ -835,6 +853,7 @@ __global__ void __launch_bounds__(Plan::MAXE >= 32 ? 256 : 1024, Plan::MAXE >= 3
 // ---------------------------------------------------------------------------
 template <class Plan, bool INV, class S, class Re>
 __global__ void __launch_bounds__(1024) k_real_odd(FftArgs a) {
+  pdl_enter();
   using SR = typename RealOf<S>::type;
   const Plan P(a.pp);
   constexpr int MAXE = Plan::MAXE;

@@ -24,17 +24,17 @@ template <class Plan, bool INV, class S, class Re>
 cudaError_t launch_c2c(const FftArgs& a, const Launch& l, bool strided, int variant) {
   if constexpr (std::is_same<S, Cx<float>>::value) {
     if (variant == 1) {
-      if (strided) return enqueue(k_c2c<Plan, INV, true, S, Re, 1, 0>, l, a);
-      return enqueue(k_c2c<Plan, INV, false, S, Re, 1, 0>, l, a);
+      if (strided) return enqueue_pdl(k_c2c<Plan, INV, true, S, Re, 1, 0>, l, a);
+      return enqueue_pdl(k_c2c<Plan, INV, false, S, Re, 1, 0>, l, a);
     }
     if (variant == 2) {
-      if (strided) return enqueue(k_c2c<Plan, INV, true, S, Re, 0, 1>, l, a);
-      return enqueue(k_c2c<Plan, INV, false, S, Re, 0, 1>, l, a);
+      if (strided) return enqueue_pdl(k_c2c<Plan, INV, true, S, Re, 0, 1>, l, a);
+      return enqueue_pdl(k_c2c<Plan, INV, false, S, Re, 0, 1>, l, a);
     }
   }
   if (variant != 0) return cudaErrorInvalidValue;
-  if (strided) return enqueue(k_c2c<Plan, INV, true, S, Re>, l, a);
-  return enqueue(k_c2c<Plan, INV, false, S, Re>, l, a);
+  if (strided) return enqueue_pdl(k_c2c<Plan, INV, true, S, Re>, l, a);
+  return enqueue_pdl(k_c2c<Plan, INV, false, S, Re>, l, a);
 }
 
 // convolution with optional spectrum output (complex64 only): variant 0 =
@@ -45,17 +45,17 @@ template <class Plan, int KOP, bool STRIDED, class S, class Re>
 cudaError_t launch_conv_layout(const FftArgs& a, const Launch& l, int variant) {
   constexpr bool C64 = std::is_same<S, Cx<float>>::value;
   if constexpr (C64 && STRIDED && IsFixPlan<Plan>::value) {
-    if (variant == 0 && l.block.x <= 256 && conv_prefetch()) return enqueue(k_conv_pf<Plan, S, Re, KOP>, l, a);
+    if (variant == 0 && l.block.x <= 256 && conv_prefetch()) return enqueue_pdl(k_conv_pf<Plan, S, Re, KOP>, l, a);
   }
   if constexpr (C64 && KOP == 0) {
-    if (variant == 1) return enqueue(k_conv<Plan, STRIDED, S, S, Re, 0, 1>, l, a);
+    if (variant == 1) return enqueue_pdl(k_conv<Plan, STRIDED, S, S, Re, 0, 1>, l, a);
   }
   if constexpr (C64 && KOP == 1) {
-    if (variant == 2) return enqueue(k_conv<Plan, STRIDED, S, S, Re, 1, 2>, l, a);
+    if (variant == 2) return enqueue_pdl(k_conv<Plan, STRIDED, S, S, Re, 1, 2>, l, a);
   }
   if (variant != 0) return cudaErrorInvalidValue;
   if constexpr (KOP == 1 && !C64) return cudaErrorInvalidValue;
-  else return enqueue(k_conv<Plan, STRIDED, S, S, Re, KOP>, l, a);
+  else return enqueue_pdl(k_conv<Plan, STRIDED, S, S, Re, KOP>, l, a);
 }
 
 template <class Plan, int KOP, class S, class Re>
@@ -69,14 +69,14 @@ template <class Plan, class S, class Re>
 cudaError_t launch_real(const FftArgs& a, const Launch& l, int op, bool with_odd) {
   switch (op) {
     case OP_R2C_EVEN:
-      return enqueue(k_r2c_even<Plan, S, Re>, l, a);
+      return enqueue_pdl(k_r2c_even<Plan, S, Re>, l, a);
     case OP_C2R_EVEN:
-      return enqueue(k_c2r_even<Plan, S, Re>, l, a);
+      return enqueue_pdl(k_c2r_even<Plan, S, Re>, l, a);
     case OP_R2C_ODD:
-      if (with_odd) return enqueue(k_real_odd<Plan, false, S, Re>, l, a);
+      if (with_odd) return enqueue_pdl(k_real_odd<Plan, false, S, Re>, l, a);
       return cudaErrorInvalidValue;
     case OP_C2R_ODD:
-      if (with_odd) return enqueue(k_real_odd<Plan, true, S, Re>, l, a);
+      if (with_odd) return enqueue_pdl(k_real_odd<Plan, true, S, Re>, l, a);
       return cudaErrorInvalidValue;
     default:
       return cudaErrorInvalidValue;

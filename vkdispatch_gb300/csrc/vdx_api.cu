@@ -1250,6 +1250,14 @@ int autotune_plan(const vdx_fft_desc& d0, vdx_plan** plan) {
 
 namespace vdx {
 
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("VDX_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 int map_plan_geometry(const vdx_fft_desc& d, MapGeometry* g) {
   Tune t;
   t.fourstep = 0;  // one CTA per transform wherever it fits

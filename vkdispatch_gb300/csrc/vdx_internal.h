@@ -189,6 +189,28 @@ inline cudaError_t enqueue(K kernel, const Launch& l, Args... args) {
   return cudaGetLastError();
 }
 
+// Programmatic dependent launch for the kernels that open with pdl_enter()
+// (fft_kernels.cuh): on unless VDX_PDL=0.
+bool pdl_enabled();
+
+template <class... KArgs, class... Args>
+inline cudaError_t enqueue_pdl(void (*kernel)(KArgs...), const Launch& l, Args... args) {
+  if (!pdl_enabled()) return enqueue(kernel, l, args...);
+  cudaError_t e = prepare_smem(kernel, l.smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = l.grid;
+  cfg.blockDim = l.block;
+  cfg.dynamicSmemBytes = l.smem;
+  cfg.stream = l.stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Geometry of a single-CTA-per-transform plan (no four-step, no Bluestein)
 // for the run-time compiled map kernels of jit.cu: the planner's pass plan,
 // launch shape and twiddle table for the descriptor's axis.
