@@ -206,3 +206,40 @@ def test_complex128_compute_with_compiled_map():
     vd.fft.fft(out, b, input_map=in_map, output_map=out_map, compute_type=vd.complex128)
     want = np.fft.fft(x * x, axis=1)
     assert rel_l2(out.read(0), want) <= 1e-12
+
+
+def test_hooks_that_do_not_compile_report_the_compiler_log():
+    """vdx_map_plan_create with C++ that NVRTC rejects returns
+    VDX_ERR_INVALID (ValueError) whose message carries the compiler's log;
+    nothing is launched."""
+    from vkdispatch_gb300 import _lib as L
+    from vkdispatch_gb300.fft import jit as J
+
+    bad = "struct VdxHooks { this is not C++; };"
+    with pytest.raises(ValueError, match="do not compile"):
+        J.get_plan((4, 64), 1, False, False, 0, L.VDX_C64, None, bad)
+
+
+def test_compiled_plan_source_and_status_reset():
+    """The compiled source is readable back, and the out-of-range status
+    resets: a map reading one element past its buffer sets it once."""
+    from vkdispatch_gb300.fft import jit as J
+
+    rng = np.random.default_rng(17)
+    x = crandn(rng, (2, 16))
+    src = vd.asbuffer(x)
+    dst = vd.Buffer((2, 16), vd.complex64)
+
+    @vd.map
+    def shifted(ib: vc.Buffer[vc.c64]):
+        op = vd.fft.read_op()
+        op.register[:] = ib[op.io_index + 1]  # the last element reads index 32 of a 32-element buffer
+
+    J.out_of_range(reset=True)
+    vd.fft.fft(dst, src, input_map=shifted)
+    assert J.out_of_range(reset=True)
+    assert not J.out_of_range()
+    shifted_x = np.concatenate([x.reshape(-1)[1:], [0]]).reshape(2, 16).astype(np.complex128)
+    assert rel_l2(dst.read(0), np.fft.fft(shifted_x, axis=1)) <= tol_fp32(16)
+    plan = next(p for k, p in J._plans.items() if "(io + (long long)(1))" in k[-1])
+    assert "vdx_mapped" in plan.source() and "FixPlan<16" in plan.source()

@@ -6,9 +6,12 @@ three-product split: an operand's hi + lo pair carries 16 significant bits,
 so a product's neglected terms are ~2^-17 of its size, about 8e-6, and the
 rounding of the FP32 accumulators and twiddles adds the usual fp32 terms.
 One 16384-point axis is four such stages plus two fp32 twiddle
-multiplications: the tests allow 3e-5 relative L2 per axis for complex64
-storage.  For bf16 / fp16 storage the rounding of the stored workspace and
-outputs dominates, exactly as on the fp32-butterfly path.
+multiplications; the neglected lo*lo terms and the accumulator rounding are
+independent between elements, so they add in quadrature.  The tests hold
+complex64 storage to the benchmark spec's 1e-5 relative L2 per 16384-point axis
+(the bench measures 7.9e-6 for the full 16384 x 16384 FFT2, both axes on the
+tensor cores).  For bf16 / fp16 storage the rounding of the stored workspace
+and outputs dominates, exactly as on the fp32-butterfly path.
 """
 
 import numpy as np
@@ -23,7 +26,7 @@ from helpers import crandn, rel_l2
 
 pytestmark = pytest.mark.gpu
 
-TC_AXIS_TOL = 3e-5  # complex64 storage, one 16384-point axis
+TC_AXIS_TOL = 1e-5  # complex64 storage, one 16384-point axis
 
 
 def _desc(shape, axis, inverse=False, normalize=0, io=L.VDX_C64, flags=L.VDX_FFT_FLAG_TENSOR_CORE):
