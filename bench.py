@@ -943,7 +943,10 @@ def batched_uneven_numbers(torch, reps=10):
     plan = BatchPlan(items, autotune=True)  # CTA size timed on scratch buffers at creation
     desc = plan.describe()
     ws = plan.make_workspace()
-    long_points = desc["long_points"]
+    # Algorithmic bytes count a second pass for the lengths above 16384 only,
+    # the most one CTA can hold, whatever split the chosen plan makes (a plan
+    # that splits more lengths moves more bytes but earns no credit for them)
+    long_points = sum(n * c for n, c in zip(lengths, counts) if n > 16384)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
 
     def timed(fn, n=reps):
@@ -1035,7 +1038,7 @@ def batched_uneven_numbers(torch, reps=10):
     torch.cuda.empty_cache()
     return {
         "items": len(items), "distinct_lengths": len(set(lengths)), "seven_smooth_sizes_in_range": nsmooth,
-        "points": points, "long_points": long_points, "plan": desc, "autotuned_cta_threads": plan.cta,
+        "points": points, "long_points": long_points, "plan_split_points": desc["long_points"], "plan": desc, "autotuned_cta_threads": plan.cta,
         "algorithmic_bytes": bytes_alg,
         "persistent_graph_ms": round(t_persist, 4),
         "persistent_GBps": round(bytes_alg / (t_persist * 1e-3) / 1e9, 1),
@@ -1294,6 +1297,73 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def batch_length_table(lengths, reps=10):
+    """Per transform length at 2^25 complex64 points: the one-item batch plan
+    at 256 threads per CTA without and with staged row tiles, and the plain
+    single-length plan of the same shape (no autotuning); median
+    CUDA-event times in microseconds and fractions of the measured HBM
+    bandwidth (16 bytes per point and pass, two passes where the plan splits
+    the length)."""
+    import torch
+
+    from vkdispatch_gb300 import _lib as L
+    from vkdispatch_gb300.batch import BatchPlan
+    from vkdispatch_gb300.fft import plan as P
+
+    torch.cuda.set_device(0)
+    peak, _ = _load_peaks()
+    total = 1 << 25
+    data = torch.randn(total + 65536, dtype=torch.complex64, device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def timed(fn):
+        x0 = data.clone()
+        fn()
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            ev[0].record()
+            fn()
+            ev[1].record()
+            torch.cuda.synchronize()
+            ts.append(ev[0].elapsed_time(ev[1]))
+        data.copy_(x0)  # repeated forward transforms grow the values
+        return statistics.median(ts)
+
+    rows = {}
+    saved = {k: os.environ.get(k) for k in ("VDX_BATCH_THREADS", "VDX_BATCH_STAGE")}
+    try:
+        for n in lengths:
+            c = total // n
+            row = {"count": c}
+            for name, stage in (("batch_direct", "0"), ("batch_staged", "3")):
+                os.environ["VDX_BATCH_THREADS"] = "256"
+                os.environ["VDX_BATCH_STAGE"] = stage
+                bp = BatchPlan([(0, n, c)])
+                ws = bp.make_workspace()
+                passes = 2 if bp.describe()["long_items"] else 1
+                t = timed(lambda: bp(data, ws))
+                row[name] = [round(t * 1e3, 1), round(passes * 16 * n * c / (t * 1e-3) / 1e9 / peak, 3)]
+            pl = P.get_plan((c, n), 1, L.VDX_KIND_C2C, False, False, L.VDX_C64, L.VDX_C64)
+            d = pl.describe()
+            ptr = data.data_ptr()
+            s = int(torch.cuda.current_stream().cuda_stream)
+            t = timed(lambda: pl.exec(ptr, ptr, None, s))
+            passes = 2 if "fourstep" in d else 1
+            row["plain"] = [round(t * 1e3, 1), round(passes * 16 * n * c / (t * 1e-3) / 1e9 / peak, 3),
+                            d.get("radices") or d.get("fourstep")]
+            rows[n] = row
+            print(n, row, file=sys.stderr, flush=True)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    print(json.dumps({"batch_length_table": rows}), flush=True)
+
+
 def run_profile(args):
     """Small fixed cases for ncu captures: a few launches of one workload,
     no timing.  conv2d = the benchmark step; c2c1024 = 32768 transforms of
@@ -1312,6 +1382,33 @@ def _run_profile(args):
     import vkdispatch_gb300 as vd
 
     torch.cuda.set_device(0)
+    if args.profile.startswith("batch_len"):
+        # one length at 2^25 points: the one-item batch plan (256 threads per
+        # CTA) and the single-length plan of the same shape, one launch each
+        from vkdispatch_gb300 import _lib as L
+        from vkdispatch_gb300.batch import BatchPlan
+        from vkdispatch_gb300.fft import plan as P
+
+        n = int(args.profile[len("batch_len"):])
+        c = (1 << 25) // n
+        data = torch.randn(n * c, dtype=torch.complex64, device="cuda")
+        os.environ["VDX_BATCH_THREADS"] = "256"
+        bp = BatchPlan([(0, n, c)])
+        ws = bp.make_workspace()
+        pl = P.get_plan((c, n), 1, L.VDX_KIND_C2C, False, False, L.VDX_C64, L.VDX_C64)
+        s = int(torch.cuda.current_stream().cuda_stream)
+        for _ in range(2):
+            bp(data, ws)
+            pl.exec(data.data_ptr(), data.data_ptr(), None, s)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("profile")
+        for _ in range(args.steps):
+            bp(data, ws)
+            pl.exec(data.data_ptr(), data.data_ptr(), None, s)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        print("profile case done", bp.describe(), pl.describe(), flush=True)
+        return
     if args.profile == "batch_uneven_2p25":
         # the batched-uneven distribution at 1/8 scale (2^25 points, 512 items)
         from vkdispatch_gb300.batch import BatchPlan, pack_items
@@ -1400,10 +1497,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip the extra configs and the CPU baseline")
+    ap.add_argument("--batch-lengths", default=None,
+                    help="comma-separated lengths: per-length batch vs single-length plan timings (JSON), then exit")
     ap.add_argument("--profile", default=None,
                     help="run a small case for ncu: conv2d, c2c<N>, diff_conv3d_256, batch_uneven_2p25, "
-                         "fs16384x4096_tc or fs16384x4096_fp32")
+                         "batch_len<N>, fs16384x4096_tc or fs16384x4096_fp32")
     args = ap.parse_args()
+    if args.batch_lengths:
+        batch_length_table([int(v) for v in args.batch_lengths.split(",")])
+        return
     if args.profile:
         run_profile(args)
         return

@@ -47,6 +47,19 @@ def test_long_lengths_four_step():
     assert d["long_items"] >= 4 and d["workspace_bytes"] > 0
 
 
+@pytest.mark.parametrize("cta", [256, 512, 1024])
+@pytest.mark.parametrize("stage,stage_t", [("0", "2"), ("3", "2"), ("7", "16")])
+def test_cta_sizes_and_staged_row_tiles(cta, stage, stage_t, monkeypatch):
+    """Every CTA size, with row tiles staged through shared memory or not:
+    narrow rows (fewer than 16 threads per transform, partial last tiles),
+    odd radices, and four-step items whose second pass stores transposed."""
+    monkeypatch.setenv("VDX_BATCH_THREADS", str(cta))
+    monkeypatch.setenv("VDX_BATCH_STAGE", stage)
+    monkeypatch.setenv("VDX_BATCH_STAGE_T", stage_t)
+    _run([(16, 257), (21, 100), (2, 9), (39, 41), (100, 33), (243, 7), (4096, 3), (12005, 1), (50421, 1),
+          (65536, 1), (8, 3)], seed=cta + int(stage))
+
+
 def test_inverse_and_unnormalised():
     _run([(512, 9), (65536, 1), (45, 3)], inverse=True, seed=2)
     _run([(512, 9), (49152, 1)], inverse=True, normalize=False, seed=3)

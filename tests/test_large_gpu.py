@@ -61,7 +61,9 @@ def _run(plan, t):
     torch.cuda.synchronize()
 
 
-@pytest.mark.parametrize("n", [8192, 12500, 16384, 20000, 24576, 32768, 65536])
+# 12005 = 245 x 49 and 50421 = 343 x 147: the first pass's last column tile
+# is partial (49 and 147 columns in tiles of 16)
+@pytest.mark.parametrize("n", [8192, 12005, 12500, 16384, 20000, 24576, 32768, 50421, 65536])
 def test_contiguous_lengths(n):
     rng = np.random.default_rng(n)
     x = crandn(rng, (3, n))

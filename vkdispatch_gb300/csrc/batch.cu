@@ -39,6 +39,21 @@ constexpr long long kWaitLimit = 1ll << 22;  // default polls of ~100 ns before 
 
 enum UnitKind { UK_ROWS = 0, UK_COLS = 1, UK_ROWS2 = 2 };
 
+// How a row unit moves its tile between global and shared memory.
+//   UF_STAGE_IN:  the tile's rows are contiguous; one coalesced copy fills
+//                 the padded row slots and the first pass gathers from them.
+//                 Used for rows held by one thread each, where every warp
+//                 load would touch 32 rows (2^25 points of length 16: 291 ->
+//                 218 us); for rows of 2-8 threads the copy and its barrier
+//                 cost more than they save (length 21: 247 -> 356 us).
+//   UF_STAGE_OUT: the same for the store of contiguous rows.
+//   UF_STAGE_OUT_T: the four-step second pass writes point k of row r at
+//                 dst + r + k * dst_pt; the results go through shared memory
+//                 and leave with adjacent rows in adjacent lanes, so each
+//                 store covers a run of rows instead of one point per row
+//                 (2^25 points of length 32768: 444 -> 363 us; 65536: 450 -> 370 us).
+enum UnitFlags { UF_STAGE_IN = 1, UF_STAGE_OUT = 2, UF_STAGE_OUT_T = 4 };
+
 struct UnitPlan {
   PassPlan pp;
   const Cx<float>* tw;  // W_n^k for this transform length
@@ -57,6 +72,8 @@ struct WorkUnit {
   int item;    // counter of a four-step item (UK_COLS signals it, UK_ROWS2 waits on it)
   int wait;    // UK_ROWS2: number of UK_COLS units of the item
   int c0;      // UK_COLS: first column of the tile
+  int flags;   // UnitFlags
+  unsigned nmag, smag;  // inv_magic(n), inv_magic(nslots): row and slot of a staged element
   float scale;
 };
 
@@ -83,6 +100,18 @@ struct UnitPlace {
   int ci, cmo, cp;  // cmo = m * cm, precomputed
   __device__ __forceinline__ int sidx(const PassPlan&, int i) const { return i * ci + cmo + (i >> 4) * cp; }
 };
+
+// Copies a tile of contiguous rows into the padded row slots of shared
+// memory: element e is point e % n of row e / n (e < M n <= 16 * 1024, so
+// the multiply-high quotient is exact).
+__device__ __forceinline__ void stage_rows_in(const Cx<float>* __restrict__ s0, Cx<float>* __restrict__ sm, int total,
+                                           int n, int npad, unsigned nmag) {
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    const int r = int(__umulhi(unsigned(e), nmag));
+    const int i = e - r * n;
+    sm[r * npad + i + (i >> 4)] = s0[e];
+  }
+}
 
 // One code path for every unit kind (separate inlined copies per kind exhaust
 // the 64 registers a thread has): the store multiplies by a per-point factor
@@ -123,23 +152,60 @@ __device__ __forceinline__ void run_unit(const BatchArgs& a, const WorkUnit* __r
   const bool active = pl.t < T && pl.m < M;
   if (!active) pl.t = 1 << 20;  // every butterfly index of an idle thread is out of range
   const bool valid = active && pl.m < wu.nslots;
-  const Cx<float>* src = (kind == UK_ROWS2 ? a.ws : a.data) + wu.src + pl.m * wu.src_slot;
+  const int flags = wu.flags;
+  // the first pass gathers point pos of slot m from src + pos * pt +
+  // (pos >> 4) * pad: the tile in global memory, or the copy the kernel loop
+  // staged into the padded row slots of shared memory (UF_STAGE_IN).  One
+  // generic-address load path: a branch between two gathers here, or a
+  // barrier inside this function, costs the kernel 400 more bytes of spills.
+  const bool stg = (flags & UF_STAGE_IN) != 0;
+  const Cx<float>* src = stg ? sm + pl.m * pp.npad : (kind == UK_ROWS2 ? a.ws : a.data) + wu.src + pl.m * wu.src_slot;
   // point offsets inside a unit stay below 2^28 (n, L1, L2 <= 16384): 32-bit
-  const int src_pt = int(wu.src_pt);
+  const int src_pt = stg ? 1 : int(wu.src_pt);
+  const int pad = stg ? 1 : 0;
   Cx<float> v[MAXE];
   radix_dispatch(pp.radix[0], [&](auto rc) {
     constexpr int RR = decltype(rc)::value;
     gather<RR, MAXE, float>(v, n / RR, T, pl.t, [&](int pos) {
       if (!valid) return mk<float>(0.f, 0.f);
-      return src[pos * src_pt];
+      return src[pos * src_pt + (pos >> 4) * pad];
     });
   });
   // row units keep each transform inside one warp when T divides 32
   run_passes<MAXE, INV>(v, pp, false, pl, sm, tw, !cols && warp_sized(T));
+  const float sc = wu.scale;
+  if (flags & (UF_STAGE_OUT | UF_STAGE_OUT_T)) {
+    __syncthreads();  // every thread's last gather from sm is done
+    radix_dispatch(pp.radix[pp.npass - 1], [&](auto rc) {
+      constexpr int RR = decltype(rc)::value;
+      each_natural<RR, MAXE, float>(v, n / RR, T, pl.t,
+                                    [&](int pos, Cx<float> val) { sm[pl.sidx(pp, pos)] = scale(val, sc); });
+    });
+    __syncthreads();
+    Cx<float>* d0 = a.data + wu.dst;
+    const int ns = wu.nslots, total = ns * n, npad = pp.npad;
+    if (flags & UF_STAGE_OUT) {
+      const unsigned nmag = wu.nmag;
+      for (int e = tid; e < total; e += blockDim.x) {
+        const int r = int(__umulhi(unsigned(e), nmag));
+        const int i = e - r * n;
+        d0[e] = sm[r * npad + i + (i >> 4)];
+      }
+    } else {
+      // point k of row r goes to d0[r + k * dst_pt]; rows fastest across lanes
+      const unsigned smag = wu.smag;
+      const int dpt = int(wu.dst_pt);
+      for (int e = tid; e < total; e += blockDim.x) {
+        const int k = ns > 1 ? int(__umulhi(unsigned(e), smag)) : e;
+        const int r = e - k * ns;
+        d0[r + k * dpt] = sm[r * npad + k + (k >> 4)];
+      }
+    }
+    return;
+  }
   Cx<float>* dst = (kind == UK_COLS ? a.ws : a.data) + wu.dst + pl.m * wu.dst_slot;
   const int dst_pt = int(wu.dst_pt);
   const bool twiddle = cols;
-  const float sc = wu.scale;
   const Cx<float>* twl = wu.twl;
   const int twstep = twiddle ? wu.c0 + pl.m : 0;  // n2; n2 * k1 < L <= 2^24
   radix_dispatch(pp.radix[pp.npass - 1], [&](auto rc) {
@@ -214,6 +280,11 @@ __global__ void __launch_bounds__(THREADS, MINB) k_batch(BatchArgs a) {
       }
       __syncthreads();
       run = s_ok != 0;
+    }
+    if (run && (wu.flags & UF_STAGE_IN)) {
+      stage_rows_in((kind == UK_ROWS2 ? a.ws : a.data) + wu.src, sm, wu.nslots * wu.pp.n, wu.pp.n, wu.pp.npad,
+                    wu.nmag);
+      __syncthreads();
     }
     if (run) run_unit<INV>(a, pu, kind, sm);
     if (kind == UK_COLS) {
@@ -325,6 +396,13 @@ int vdx_batch_plan_create(const vdx_batch_item* items, int nitems, int inverse, 
   int cta = 512;
   if (const char* ev = std::getenv("VDX_BATCH_THREADS")) cta = std::atoi(ev);
   if (cta != 256 && cta != 512 && cta != 1024) return set_error(VDX_ERR_INVALID, "VDX_BATCH_THREADS must be 256, 512 or 1024");
+  // row tiles staged through shared memory (UnitFlags).  VDX_BATCH_STAGE is a
+  // mask: 1 = rows of fewer than VDX_BATCH_STAGE_T threads (whole-length
+  // items), 2 = the transposed store of four-step second passes, 4 = their
+  // input rows of fewer than VDX_BATCH_STAGE_T threads
+  int stage = 3, stage_t = 2;
+  if (const char* ev = std::getenv("VDX_BATCH_STAGE")) stage = std::atoi(ev);
+  if (const char* ev = std::getenv("VDX_BATCH_STAGE_T")) stage_t = std::atoi(ev);
   const int per_sm = 1024 / cta;  // 64 registers per thread at any of the three sizes
   // shared memory per CTA so that per_sm CTAs fit on one SM
   const int smem_cap = std::min(smem_optin, smem_sm / per_sm - 1024);
@@ -397,6 +475,10 @@ int vdx_batch_plan_create(const vdx_batch_item* items, int nitems, int inverse, 
         w.nslots = (int)std::min<long long>(M, it.count - t0);
         w.item = -1;
         w.scale = scale;
+        // narrow rows (fewer than 16 threads each) move through shared memory
+        if ((stage & 1) && L >= 2 && plans[p].pp.T < stage_t) w.flags = UF_STAGE_IN | UF_STAGE_OUT;
+        w.nmag = inv_magic(L);
+        w.smag = inv_magic(w.nslots);
         w.twl = plans[p].tw;  // valid pointer; only column units read it
         rows_units.push_back(w);
       }
@@ -453,6 +535,13 @@ int vdx_batch_plan_create(const vdx_batch_item* items, int nitems, int inverse, 
         w.nslots = std::min(Mr, L1 - r0);
         w.item = item;
         w.scale = scale;
+        // the transposed store goes through shared memory wherever a unit holds several rows
+        if (L2 >= 2) {
+          if ((stage & 2) && w.nslots > 1) w.flags |= UF_STAGE_OUT_T;
+          if ((stage & 4) && plans[pr].pp.T < stage_t) w.flags |= UF_STAGE_IN;
+        }
+        w.nmag = inv_magic(L2);
+        w.smag = inv_magic(w.nslots);
         w.twl = plans[pr].tw;  // valid pointer; only column units read it
         rows2_units.push_back(w);
       }

@@ -146,7 +146,8 @@ __device__ __forceinline__ void fused_tile(const Plan& P, const TilePlace& pl, c
     P.template last<false>([&](auto rc) {
       constexpr int RR = decltype(rc)::value;
       each_natural<RR, MAXE, float>(v, n / RR, P.T(), pl.t, [&](int pos, Cx<float> val) {
-        const Cx<float> w = ldg(twl + (long long)(col0 + pl.m) * pos);
+        // columns past ncols take exponent 0 (their products would index past the table)
+        const Cx<float> w = ldg(twl + (valid ? (long long)(col0 + pl.m) * pos : 0ll));
         sm[pl.m * ld + pos] = INV ? cmulc(val, w) : cmul(val, w);
       });
     });

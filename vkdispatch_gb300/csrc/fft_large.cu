@@ -153,9 +153,11 @@ __global__ void __launch_bounds__(512) k_fs(const __grid_constant__ CUtensorMap 
       });
     });
   } else {
-    // W_N^{b0 k1}: b0 < N0 and k1 = pos < N1, so the exponent is below N
+    // W_N^{b0 k1}: b0 < N0 and k1 = pos < N1, so the exponent is below N.
+    // Columns past the last one of a partial tile (col >= ncols) take b0 = 0:
+    // their products would index past the table's N entries
     const Cx<Re>* twl = reinterpret_cast<const Cx<Re>*>(a.twl);
-    const int b0 = a.tw_from_batch ? (int)br : col;
+    const int b0 = a.tw_from_batch ? (int)br : (valid ? col : 0);
     if constexpr (MODE == 1) {
       const long long ops = a.out_ps;
       P.template last<false>([&](auto rc) {

@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(kTcThreads) k_fs_tc(FsArgs a, const unsigned c
       float x[16];
       tc::tmem_ld16(lane_base + 16 * t, x);
       // W_N^{b0 k}: b0 < N0 and k = pos < N1, so the exponent is below N
-      const int b0 = a.tw_from_batch ? (int)br : col;
+      const int b0 = a.tw_from_batch ? (int)br : (valid ? col : 0);  // no table index past N for absent columns
 #pragma unroll
       for (int k2 = 0; k2 < 8; ++k2) {
         const int pos = k1 + 16 * k2;
