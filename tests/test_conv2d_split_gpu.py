@@ -1,0 +1,105 @@
+"""convolve2DR over a batch of images split into groups, each group's
+rfft -> convolution -> irfft chain on its own stream (fft/functions.py
+_conv2d_split): the same results as one group on the caller's stream, for
+replicated and broadcast kernels, uneven groups, CUDA-graph capture and
+deferred CommandGraph recording."""
+
+import numpy as np
+import pytest
+import torch
+
+import vkdispatch_gb300 as vd
+
+from helpers import rel_l2, tol_fp32
+
+pytestmark = pytest.mark.gpu
+
+TOL = 4 * tol_fp32(512)
+
+
+def _gaussian_spectrum(H, W, sigma=5.0, size=31):
+    ax = np.arange(size) - size // 2
+    g = np.exp(-(ax[:, None] ** 2 + ax[None, :] ** 2) / (2 * sigma ** 2))
+    k = np.zeros((H, W))
+    k[:size, :size] = g / g.sum()
+    return np.fft.rfft2(k)
+
+
+def _ref(x, K):
+    S = np.fft.rfft(x.astype(np.float64), axis=-1)
+    T = np.fft.ifft(np.fft.fft(S, axis=-2) * np.conj(K), axis=-2)
+    return np.fft.irfft(T, n=x.shape[-1], axis=-1)
+
+
+def _inputs(n, seed, broadcast=False):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1, 1, (n, 512, 512)).astype(np.float32)
+    if broadcast:
+        K = _gaussian_spectrum(512, 512)
+        kb = vd.RFFTBuffer((1, 512, 512))
+        kb.write_fourier(K.astype(np.complex64)[None])
+    else:
+        K = (rng.standard_normal((n, 512, 257)) + 1j * rng.standard_normal((n, 512, 257))) * 0.01
+        kb = vd.RFFTBuffer((n, 512, 512))
+        kb.write_fourier(K.astype(np.complex64))
+    buf = vd.RFFTBuffer((n, 512, 512))
+    buf.write_real(x)
+    return x, K, buf, kb
+
+
+def _conv(buf, kb, parts, monkeypatch, **kw):
+    monkeypatch.setenv("VDX_CONV2D_STREAMS", str(parts))
+    vd.fft.convolve2DR(buf, kb, **kw)
+    torch.cuda.synchronize()
+    return buf.tensor.cpu().numpy()
+
+
+@pytest.mark.parametrize("n,parts", [(16, 2), (18, 4), (24, 3)])
+def test_groups_match_one_group(n, parts, monkeypatch):
+    x, K, buf, kb = _inputs(n, n + parts)
+    got = _conv(buf, kb, parts, monkeypatch)
+    buf.write_real(x)
+    one = _conv(buf, kb, 1, monkeypatch)
+    assert rel_l2(got, one) <= TOL
+    buf.tensor.copy_(torch.from_numpy(got))
+    assert rel_l2(buf.read_real(0), _ref(x, K)) <= TOL
+
+
+def test_broadcast_kernel(monkeypatch):
+    x, K, buf, kb = _inputs(16, 7, broadcast=True)
+    got = _conv(buf, kb, 2, monkeypatch, kernel_inner_only=True)
+    buf.write_real(x)
+    one = _conv(buf, kb, 1, monkeypatch, kernel_inner_only=True)
+    assert rel_l2(got, one) <= TOL
+    assert rel_l2(buf.read_real(0), _ref(x, K)) <= TOL
+
+
+def test_cuda_graph_capture(monkeypatch):
+    monkeypatch.setenv("VDX_CONV2D_STREAMS", "2")
+    x, K, buf, kb = _inputs(16, 8)
+    vd.fft.convolve2DR(buf, kb)  # plans created before capture
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            with vd.cuda_graph_capture(torch.cuda.current_stream()):
+                vd.fft.convolve2DR(buf, kb)
+    torch.cuda.current_stream().wait_stream(s)
+    buf.write_real(x)
+    g.replay()
+    torch.cuda.synchronize()
+    assert rel_l2(buf.read_real(0), _ref(x, K)) <= TOL
+
+
+def test_deferred_command_graph(monkeypatch):
+    monkeypatch.setenv("VDX_CONV2D_STREAMS", "2")
+    x, K, buf, kb = _inputs(16, 9)
+    cg = vd.CommandGraph()
+    vd.fft.convolve2DR(buf, kb, graph=cg)
+    torch.cuda.synchronize()
+    assert rel_l2(buf.read_real(0), x) == 0.0  # nothing ran yet
+    cg.submit()
+    torch.cuda.synchronize()
+    assert rel_l2(buf.read_real(0), _ref(x, K)) <= TOL
