@@ -181,7 +181,7 @@ struct Tune {
   int order = 0;      // radix passes: 0 = largest radix first, 1 = smallest first
   int fixed = -1;     // compile-time kernels where available: -1 = yes, 0 = no
   int fourstep = -1;  // long C2C axes: -1 = from 8192 points (VDX_FOURSTEP_MIN), 0 = only above one CTA, 1 = always
-  int maxe = 16;      // points per thread: 16, or 8 / 32 (strided complex64 convolutions with a compile-time plan)
+  int maxe = 0;       // points per thread: 0 = the plan's default, or 16 / 8 / 32 (compile-time plans where they exist)
 };
 }  // namespace vdx
 
@@ -850,8 +850,13 @@ int create_plan(const vdx_fft_desc* desc, const Tune& tune, vdx_plan** plan) {
                       std::getenv("VDX_NO_FIXED") == nullptr;
   const bool is_conv = d.kind == VDX_KIND_CONV;
   int pmaxe = (tune.maxe == 8 || tune.maxe == 32) ? tune.maxe : 16;
+  // default for strided complex64 convolutions of 512 or 1024 points: the
+  // two-pass radix-32 plan (64 x 512 x 257 along axis 1: 58.0 us against
+  // 70.3 us for radix 16 x 16 x 2, each launch alone from a cold L2)
+  if (tune.maxe == 0 && is_conv && inner > 1 && canpts && has_fixedpts_c64(n, 32, true, true)) pmaxe = 32;
   if (const char* e = std::getenv("VDX_POINTS_PER_THREAD")) {
     const int v = std::atoi(e);
+    if (v == 16) pmaxe = 16;
     if ((v == 8 || v == 32) && canpts && has_fixedpts_c64(n, v, is_conv, inner > 1)) pmaxe = v;
   }
   if (pmaxe != 16 && !(canpts && has_fixedpts_c64(n, pmaxe, is_conv, inner > 1))) {
@@ -1189,10 +1194,11 @@ int autotune_plan(const vdx_fft_desc& d0, vdx_plan** plan) {
             t.fourstep = fsv;
             cands.push_back(t);
           }
-    // the 8- and 32-points-per-thread compile-time plans (create_plan
-    // refuses the combinations that have none)
+    // the 8-, 16- and 32-points-per-thread plans (16 differs from the
+    // default only where the default is 32: strided convolutions of 512 or
+    // 1024 points; create_plan refuses the combinations that have none)
     if (d.io_type == VDX_C64 && d.compute_type == VDX_C64)
-      for (int pts : {8, 32})
+      for (int pts : {8, 16, 32})
         for (int w : widths) {
           Tune t;
           t.width = w;
@@ -1350,7 +1356,7 @@ int vdx_autotune_load(const char* path) {
     t.order = v[13];
     t.fixed = v[14];
     t.fourstep = v[15];
-    t.maxe = (v[16] == 8 || v[16] == 32) ? v[16] : 16;
+    t.maxe = (v[16] == 8 || v[16] == 16 || v[16] == 32) ? v[16] : 0;
     g_tuned[k] = t;
     ++loaded;
   }
