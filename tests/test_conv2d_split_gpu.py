@@ -103,3 +103,57 @@ def test_deferred_command_graph(monkeypatch):
     cg.submit()
     torch.cuda.synchronize()
     assert rel_l2(buf.read_real(0), _ref(x, K)) <= TOL
+
+
+def _crand(rng, shape):
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+
+
+@pytest.mark.parametrize("parts", [2, 3])
+def test_rfft2_irfft2_groups(parts, monkeypatch):
+    rng = np.random.default_rng(20 + parts)
+    x = rng.uniform(-1, 1, (16, 512, 512)).astype(np.float32)
+    buf = vd.RFFTBuffer(x.shape)
+    buf.write_real(x)
+    monkeypatch.setenv("VDX_CONV2D_STREAMS", str(parts))
+    vd.fft.rfft2(buf)
+    torch.cuda.synchronize()
+    spec = buf.read_fourier(0)
+    assert rel_l2(spec, np.fft.rfft2(x.astype(np.float64))) <= 2 * tol_fp32(512)
+    vd.fft.irfft2(buf)
+    torch.cuda.synchronize()
+    assert rel_l2(buf.read_real(0), x) <= 4 * tol_fp32(512)
+
+
+@pytest.mark.parametrize("parts", [2, 4])
+def test_fft2_ifft2_and_convolve2d_groups(parts, monkeypatch):
+    rng = np.random.default_rng(30 + parts)
+    x = _crand(rng, (16, 256, 512))
+    K = _crand(rng, (16, 256, 512)) * 0.05
+    buf = vd.asbuffer(x)
+    monkeypatch.setenv("VDX_CONV2D_STREAMS", str(parts))
+    vd.fft.fft2(buf)
+    torch.cuda.synchronize()
+    assert rel_l2(buf.read(0), np.fft.fft2(x.astype(np.complex128))) <= 2 * tol_fp32(256, 512)
+    vd.fft.ifft2(buf)
+    torch.cuda.synchronize()
+    assert rel_l2(buf.read(0), x) <= 4 * tol_fp32(256, 512)
+    kb = vd.asbuffer(K)
+    vd.fft.convolve2D(buf, kb)
+    torch.cuda.synchronize()
+    x64 = x.astype(np.complex128)
+    S = np.fft.fft(x64, axis=2)
+    ref = np.fft.ifft(np.fft.ifft(np.fft.fft(S, axis=1) * np.conj(K), axis=1), axis=2)
+    assert rel_l2(buf.read(0), ref) <= 4 * tol_fp32(256, 512)
+
+
+def test_long_axes_keep_one_group(monkeypatch):
+    """Axes of 8192 points and up plan as four-step pairs that own a
+    workspace: those chains stay on the caller's stream."""
+    rng = np.random.default_rng(40)
+    x = _crand(rng, (8, 64, 16384))
+    buf = vd.asbuffer(x)
+    monkeypatch.setenv("VDX_CONV2D_STREAMS", "2")
+    vd.fft.fft2(buf)
+    torch.cuda.synchronize()
+    assert rel_l2(buf.read(0), np.fft.fft2(x.astype(np.complex128))) <= 2 * tol_fp32(64, 16384)

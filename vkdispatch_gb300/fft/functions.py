@@ -314,6 +314,11 @@ def fft2(buffer: Buffer, graph=None, print_shader=False, input_map=None, output_
          input_type=None, compute_type=None):
     if len(buffer.shape) not in (2, 3):
         raise ValueError("Buffer must have 2 or 3 dimensions")
+    if (input_map is None and output_map is None and output_type in (None, dt.complex64)
+            and input_type in (None, dt.complex64) and compute_type in (None, dt.complex64) and _groupable(buffer)
+            and _axes_split(buffer, [(L.VDX_KIND_C2C, 1, False, False, None), (L.VDX_KIND_C2C, 2, False, False, None)],
+                            graph, print_shader)):
+        return
     kw = dict(graph=graph, print_shader=print_shader, output_type=output_type, input_type=input_type,
               compute_type=compute_type)
     fft(buffer, axis=len(buffer.shape) - 2, input_map=input_map, **kw)
@@ -342,6 +347,11 @@ def ifft2(buffer: Buffer, graph=None, print_shader=False, normalize=True, input_
           output_type=None, input_type=None, compute_type=None):
     if len(buffer.shape) not in (2, 3):
         raise ValueError("Buffer must have 2 or 3 dimensions")
+    if (input_map is None and output_map is None and output_type in (None, dt.complex64)
+            and input_type in (None, dt.complex64) and compute_type in (None, dt.complex64) and _groupable(buffer)
+            and _axes_split(buffer, [(L.VDX_KIND_C2C, 1, True, bool(normalize), None),
+                                     (L.VDX_KIND_C2C, 2, True, bool(normalize), None)], graph, print_shader)):
+        return
     kw = dict(graph=graph, print_shader=print_shader, normalize=normalize, output_type=output_type,
               input_type=input_type, compute_type=compute_type)
     ifft(buffer, axis=len(buffer.shape) - 2, input_map=input_map, **kw)
@@ -367,6 +377,10 @@ def rfft(buffer: RFFTBuffer, graph=None, print_shader=False, name=None, compute_
 def rfft2(buffer: RFFTBuffer, graph=None, print_shader=False, compute_type=None):
     if len(buffer.real_shape) not in (2, 3):
         raise ValueError("Buffer must have 2 or 3 dimensions")
+    if (compute_type in (None, dt.complex64) and len(buffer.real_shape) == 3 and _groupable(buffer)
+            and _axes_split(buffer, [(L.VDX_KIND_R2C, 2, False, False, buffer.real_shape),
+                                     (L.VDX_KIND_C2C, 1, False, False, None)], graph, print_shader)):
+        return
     rfft(buffer, graph=graph, print_shader=print_shader, compute_type=compute_type)
     fft(buffer, graph=graph, print_shader=print_shader, axis=len(buffer.real_shape) - 2,
         output_type=buffer.var_type, input_type=buffer.var_type, compute_type=compute_type)
@@ -390,6 +404,11 @@ def irfft(buffer: RFFTBuffer, graph=None, print_shader=False, name=None, normali
 def irfft2(buffer: RFFTBuffer, graph=None, print_shader=False, normalize=True, compute_type=None):
     if len(buffer.real_shape) not in (2, 3):
         raise ValueError("Buffer must have 2 or 3 dimensions")
+    if (compute_type in (None, dt.complex64) and len(buffer.real_shape) == 3 and _groupable(buffer)
+            and _axes_split(buffer, [(L.VDX_KIND_C2C, 1, True, bool(normalize), None),
+                                     (L.VDX_KIND_C2R, 2, True, bool(normalize), buffer.real_shape)], graph,
+                            print_shader)):
+        return
     ifft(buffer, graph=graph, print_shader=print_shader, axis=len(buffer.real_shape) - 2, normalize=normalize,
          output_type=buffer.var_type, input_type=buffer.var_type, compute_type=compute_type)
     irfft(buffer, graph=graph, print_shader=print_shader, normalize=normalize, compute_type=compute_type)
@@ -742,6 +761,30 @@ def convolve2D(buffer: Buffer, kernel: Buffer, kernel_map=None, buffer_shape=Non
                output_type=None, input_type=None, kernel_type=None, compute_type=None):
     if len(buffer.shape) not in (2, 3):
         raise ValueError("Buffer must have 2 or 3 dimensions")
+    if (kernel_map is None and buffer_shape is None and not transposed_kernel and input_map is None
+            and output_map is None and output_type in (None, dt.complex64) and input_type in (None, dt.complex64)
+            and kernel_type in (None, dt.complex64) and compute_type in (None, dt.complex64)
+            and _groupable(buffer, kernel) and len(buffer.shape) == 3):
+        img = math.prod(buffer.shape[1:])
+        broadcast = bool(kernel_inner_only)
+        if not broadcast and kernel.size < buffer.size:
+            if kernel.size < img:
+                raise ValueError(f"kernel buffer of {kernel.size} elements is smaller than the signal "
+                                 f"({buffer.size})")
+            broadcast = True
+
+        def build(b0, nb):
+            shape = (nb,) + tuple(int(x) for x in buffer.shape[1:])
+            ptr = buffer.ptr + b0 * img * 8
+            kptr = kernel.ptr if broadcast else kernel.ptr + b0 * img * 8
+            return [(P.get_plan(shape, 2, L.VDX_KIND_C2C, False, False, L.VDX_C64, L.VDX_C64, None), ptr, ptr, None),
+                    (P.get_plan(shape, 1, L.VDX_KIND_CONV, False, bool(normalize), L.VDX_C64, L.VDX_C64, None,
+                                L.VDX_KOP_MUL_CONJ, L.VDX_C64, broadcast), ptr, ptr, kptr),
+                    (P.get_plan(shape, 2, L.VDX_KIND_C2C, True, bool(normalize), L.VDX_C64, L.VDX_C64, None), ptr,
+                     ptr, None)]
+
+        if _image_groups(buffer, graph, (buffer, kernel), build, print_shader):
+            return
     fft(buffer, graph=graph, print_shader=print_shader, input_map=input_map, output_type=output_type,
         input_type=input_type, compute_type=compute_type)
     convolve(buffer, kernel, kernel_map=kernel_map, buffer_shape=buffer_shape, graph=graph,
@@ -804,46 +847,36 @@ def _conv2d_split_parts() -> int:
         return 2
 
 
-def _conv2d_split(buffer, kernel, kernel_inner_only, normalize, graph, print_shader) -> bool:
-    """A batch of 2-D images runs as `parts` groups of images, each group's
-    rfft -> column convolution -> irfft chain on its own stream, forked from
-    and joined back into the caller's stream.  Every kernel of the step is
+def _image_groups(buffer, graph, keep, build, print_shader=False) -> bool:
+    """Runs a batch of 2-D images as `parts` groups of images, each group's
+    chain of launches on its own library-owned stream, forked from and
+    joined back into the caller's stream.  Every kernel of such a chain is
     latency-bound at partial occupancy, so one group's kernels fill the SMs
-    that another group's kernel leaves idle while it drains (64 x 512^2 on
-    GB300: 0.1087-0.1099 ms for two groups of 32 against 0.1152-0.1167 ms for
-    one group of 64, untuned plans).  The results are those of one group:
-    each image's chain is the same.  Returns False when the caller must run
-    the three transforms over the whole batch: fewer than 8 images, less
-    than 16 MiB, or VDX_CONV2D_STREAMS=1."""
+    that another group's kernel leaves idle while it drains (convolve2DR of
+    64 x 512^2 on GB300: 0.0954 ms for two groups of 32 against 0.1019 ms for
+    one group of 64).  Each image goes through the same plans' arithmetic, so
+    the results are those of one group.
+
+    build(b0, nb) returns the plans of images [b0, b0 + nb) as a list of
+    (plan, in_ptr, out_ptr, ker_ptr).  Returns False (nothing recorded) for a
+    buffer that is not a batch of at least 8 images of 16 MiB or more in all,
+    or with VDX_CONV2D_STREAMS=1."""
     import torch
 
     parts = _conv2d_split_parts()
-    real_shape = tuple(int(x) for x in buffer.real_shape)
-    if parts < 2 or len(real_shape) != 3 or real_shape[0] < 8 or buffer.mem_size < (16 << 20):
+    if parts < 2 or len(buffer.shape) != 3 or int(buffer.shape[0]) < 8 or buffer.mem_size < (16 << 20):
         return False
-    nimg = real_shape[0]
+    nimg = int(buffer.shape[0])
     parts = min(parts, nimg // 4)
-    img = math.prod(buffer.shape[1:])  # complex elements per image
-    broadcast = bool(kernel_inner_only)
-    if not broadcast and kernel.size < buffer.size:
-        if kernel.size < img:
-            raise ValueError(f"kernel buffer of {kernel.size} elements is smaller than the signal ({buffer.size})")
-        broadcast = True
     cut = [nimg * i // parts for i in range(parts + 1)]
-    groups = []
-    for i in range(parts):
-        b0, nb = cut[i], cut[i + 1] - cut[i]
-        rs = (nb,) + real_shape[1:]
-        fs = (nb,) + tuple(int(x) for x in buffer.shape[1:])
-        fwd = P.get_plan(rs, 2, L.VDX_KIND_R2C, False, False, L.VDX_C64, L.VDX_C64, None)
-        conv = P.get_plan(fs, 1, L.VDX_KIND_CONV, False, bool(normalize), L.VDX_C64, L.VDX_C64, None,
-                          L.VDX_KOP_MUL_CONJ, L.VDX_C64, broadcast)
-        inv = P.get_plan(rs, 2, L.VDX_KIND_C2R, True, bool(normalize), L.VDX_C64, L.VDX_C64, None)
-        ptr = buffer.ptr + b0 * img * 8
-        kptr = kernel.ptr if broadcast else kernel.ptr + b0 * img * 8
-        groups.append((fwd, conv, inv, ptr, kptr))
-        if print_shader:
-            print(fwd.describe(), conv.describe(), inv.describe())
+    groups = [build(cut[i], cut[i + 1] - cut[i]) for i in range(parts)]
+    # groups of equal size share plans, and a plan that owns a workspace
+    # (four-step and Bluestein axes) must not run on two streams at once
+    if any(_owns_workspace(pl) for g in groups for pl, *_ in g):
+        return False
+    if print_shader:
+        for g in groups:
+            print(*(pl.describe() for pl, *_ in g))
     dev = torch_device_index()
     st = _split_streams.get((dev, parts))
     if st is None:
@@ -856,16 +889,72 @@ def _conv2d_split(buffer, kernel, kernel_inner_only, normalize, graph, print_sha
     def launch(s):
         caller = torch.cuda.ExternalStream(s) if s else torch.cuda.current_stream()
         fork.record(caller)
-        for side, h, join, (fwd, conv, inv, ptr, kptr) in zip(sides, handles, joins, groups):
+        for side, h, join, g in zip(sides, handles, joins, groups):
             side.wait_event(fork)
-            fwd.exec(ptr, ptr, None, h)
-            conv.exec(ptr, ptr, kptr, h)
-            inv.exec(ptr, ptr, None, h)
+            for pl, src, dst, ker in g:
+                pl.exec(src, dst, ker, h)
             join.record(side)
             caller.wait_event(join)
 
-    _record(graph, launch, (buffer, kernel))
+    _record(graph, launch, keep)
     return True
+
+
+def _owns_workspace(plan) -> bool:
+    ws = getattr(plan, "_owns_workspace", None)
+    if ws is None:
+        d = plan.describe()
+        ws = "fourstep" in d or "bluestein" in d
+        plan._owns_workspace = ws
+    return ws
+
+
+def _groupable(*buffers) -> bool:
+    """complex64 storage, contiguous: the buffers the image-group split takes."""
+    return all(b.var_type == dt.complex64 and b.contiguous for b in buffers)
+
+
+def _conv2d_split(buffer, kernel, kernel_inner_only, normalize, graph, print_shader) -> bool:
+    """convolve2DR as image groups: rfft rows -> column convolution -> irfft
+    rows per group (see _image_groups)."""
+    real_shape = tuple(int(x) for x in buffer.real_shape)
+    if len(real_shape) != 3:
+        return False
+    img = math.prod(buffer.shape[1:])  # complex elements per image
+    broadcast = bool(kernel_inner_only)
+    if not broadcast and kernel.size < buffer.size:
+        if kernel.size < img:
+            raise ValueError(f"kernel buffer of {kernel.size} elements is smaller than the signal ({buffer.size})")
+        broadcast = True
+
+    def build(b0, nb):
+        rs = (nb,) + real_shape[1:]
+        fs = (nb,) + tuple(int(x) for x in buffer.shape[1:])
+        ptr = buffer.ptr + b0 * img * 8
+        kptr = kernel.ptr if broadcast else kernel.ptr + b0 * img * 8
+        return [(P.get_plan(rs, 2, L.VDX_KIND_R2C, False, False, L.VDX_C64, L.VDX_C64, None), ptr, ptr, None),
+                (P.get_plan(fs, 1, L.VDX_KIND_CONV, False, bool(normalize), L.VDX_C64, L.VDX_C64, None,
+                            L.VDX_KOP_MUL_CONJ, L.VDX_C64, broadcast), ptr, ptr, kptr),
+                (P.get_plan(rs, 2, L.VDX_KIND_C2R, True, bool(normalize), L.VDX_C64, L.VDX_C64, None), ptr, ptr,
+                 None)]
+
+    return _image_groups(buffer, graph, (buffer, kernel), build, print_shader)
+
+
+def _axes_split(buffer, steps, graph, print_shader) -> bool:
+    """A chain of per-image transforms of a (batch, H, W) buffer as image
+    groups; steps = [(kind, axis, inverse, normalize, real_shape_or_None)]."""
+    img = math.prod(buffer.shape[1:])
+
+    def build(b0, nb):
+        ptr = buffer.ptr + b0 * img * 8
+        out = []
+        for kind, ax, inv, norm, real in steps:
+            shape = (nb,) + tuple(int(x) for x in (real if real is not None else buffer.shape)[1:])
+            out.append((P.get_plan(shape, ax, kind, inv, norm, L.VDX_C64, L.VDX_C64, None), ptr, ptr, None))
+        return out
+
+    return _image_groups(buffer, graph, (buffer,), build, print_shader)
 
 
 def torch_device_index() -> int:
@@ -885,7 +974,7 @@ def convolve2DR(buffer: RFFTBuffer, kernel: RFFTBuffer, kernel_map=None, buffer_
         return
     if (kernel_map is None and buffer_shape is None and not transposed_kernel
             and compute_type in (None, dt.complex64) and buffer.var_type == dt.complex64
-            and kernel.var_type == dt.complex64 and buffer.contiguous and kernel.contiguous
+            and _groupable(buffer, kernel)
             and _conv2d_split(buffer, kernel, kernel_inner_only, normalize, graph, print_shader)):
         return
     rfft(buffer, graph=graph, print_shader=print_shader, compute_type=compute_type)
