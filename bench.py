@@ -1477,7 +1477,10 @@ def _run_profile(args):
         torch.cuda.synchronize()
         print("profile case done", flush=True)
         return
-    if args.profile == "conv2d":
+    if args.profile in ("conv2d", "conv2d_kernels"):
+        # conv2d: the public call (two image groups on two streams);
+        # conv2d_kernels: the three kernels over all 64 images on one stream,
+        # as the bench's per-kernel pass runs them
         images, kernel = make_inputs()
         kb = vd.asrfftbuffer(kernel)
         vd.fft.rfft2(kb)
@@ -1485,11 +1488,20 @@ def _run_profile(args):
         kspec.tensor.copy_(kb.tensor.unsqueeze(0).expand(B, H, HC))
         buf = vd.RFFTBuffer((B, H, W))
         buf.write_real(images)
-        vd.fft.convolve2DR(buf, kspec)  # plans (and their tuning) before the range
+        def step():
+            if args.profile == "conv2d":
+                vd.fft.convolve2DR(buf, kspec)
+                return
+            vd.fft.rfft(buf)
+            vd.fft.convolve(buf, kspec, axis=1, output_type=buf.var_type, input_type=buf.var_type,
+                            kernel_type=kspec.var_type)
+            vd.fft.irfft(buf)
+
+        step()  # plans (and their tuning) before the range
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_push("profile")
         for _ in range(args.steps):
-            vd.fft.convolve2DR(buf, kspec)
+            step()
         torch.cuda.nvtx.range_pop()
     else:
         n = int(args.profile[3:])
@@ -1517,7 +1529,7 @@ def main():
     ap.add_argument("--batch-lengths", default=None,
                     help="comma-separated lengths: per-length batch vs single-length plan timings (JSON), then exit")
     ap.add_argument("--profile", default=None,
-                    help="run a small case for ncu: conv2d, c2c<N>, diff_conv3d_256, batch_uneven_2p25, "
+                    help="run a small case for ncu: conv2d, conv2d_kernels, c2c<N>, diff_conv3d_256, batch_uneven_2p25, "
                          "batch_len<N>, fs16384x4096_tc or fs16384x4096_fp32")
     args = ap.parse_args()
     if args.batch_lengths:
