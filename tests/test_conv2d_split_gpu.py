@@ -157,3 +157,40 @@ def test_long_axes_keep_one_group(monkeypatch):
     vd.fft.fft2(buf)
     torch.cuda.synchronize()
     assert rel_l2(buf.read(0), np.fft.fft2(x.astype(np.complex128))) <= 2 * tol_fp32(64, 16384)
+
+
+def test_two_host_threads(monkeypatch):
+    """Each host thread forks its own side streams and events: concurrent
+    calls from two threads on their own torch streams keep their results."""
+    import threading
+
+    monkeypatch.setenv("VDX_CONV2D_STREAMS", "2")
+    cases = [_inputs(16, 50 + i) for i in range(2)]
+    for _, _, buf, kb in cases:  # plans created before the threads start
+        vd.fft.convolve2DR(buf, kb)
+    torch.cuda.synchronize()
+    for x, _, buf, _ in cases:
+        buf.write_real(x)
+    errors = []
+
+    def work(i):
+        try:
+            x, K, buf, kb = cases[i]
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                for _ in range(3):
+                    buf.write_real(x)
+                    vd.fft.convolve2DR(buf, kb)
+            s.synchronize()
+        except Exception as e:  # reported by the main thread
+            errors.append(e)
+
+    ts = [threading.Thread(target=work, args=(i,)) for i in range(2)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors
+    torch.cuda.synchronize()
+    for x, K, buf, _ in cases:
+        assert rel_l2(buf.read_real(0), _ref(x, K)) <= TOL

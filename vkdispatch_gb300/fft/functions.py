@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import math
 import os
+import threading
 from typing import Optional, Tuple, Union
 
 import numpy as np
@@ -834,7 +835,10 @@ def _conv2d_fused(buffer, kernel, kernel_inner_only, normalize, graph, print_sha
     return True
 
 
-_split_streams = {}  # device -> (side streams, fork event, join events)
+# per host thread: (device, parts) -> (side streams, fork event, join events).
+# The fork and join events are re-recorded by every call, so two host
+# threads must not share them.
+_split_tls = threading.local()
 
 
 def _conv2d_split_parts() -> int:
@@ -878,11 +882,14 @@ def _image_groups(buffer, graph, keep, build, print_shader=False) -> bool:
         for g in groups:
             print(*(pl.describe() for pl, *_ in g))
     dev = torch_device_index()
-    st = _split_streams.get((dev, parts))
+    cache = getattr(_split_tls, "streams", None)
+    if cache is None:
+        cache = _split_tls.streams = {}
+    st = cache.get((dev, parts))
     if st is None:
         st = ([torch.cuda.Stream(device=dev) for _ in range(parts)], torch.cuda.Event(),
               [torch.cuda.Event() for _ in range(parts)])
-        _split_streams[(dev, parts)] = st
+        cache[(dev, parts)] = st
     sides, fork, joins = st
     handles = [int(x.cuda_stream) for x in sides]
 
