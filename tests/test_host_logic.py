@@ -291,3 +291,39 @@ def test_torch_fft_front_end_resize():
     assert q.shape == (3, 6) and torch.equal(q[:, :4], x) and torch.all(q[:, 4:] == 0)
     with pytest.raises(ValueError):
         tf._resize(x, 1, 0)
+
+
+@pytest.mark.parametrize("value,parts", [(None, 2), ("3", 3), ("1", 1), ("0", 1), ("20", 8), ("x", 2)])
+def test_image_group_count_setting(monkeypatch, value, parts):
+    """VDX_CONV2D_STREAMS: image groups of the batched 2-D transforms, 1-8."""
+    from vkdispatch_gb300.fft import functions as F
+
+    if value is None:
+        monkeypatch.delenv("VDX_CONV2D_STREAMS", raising=False)
+    else:
+        monkeypatch.setenv("VDX_CONV2D_STREAMS", value)
+    assert F._conv2d_split_parts() == parts
+
+
+def test_image_groups_refuse_small_batches_without_gpu(monkeypatch):
+    """Batches of fewer than 8 images, or under 16 MiB, or one group: nothing
+    is recorded and the caller runs the whole batch itself."""
+    from vkdispatch_gb300.fft import functions as F
+
+    class FakeBuf:
+        def __init__(self, shape):
+            self.shape = shape
+            n = 8
+            for d in shape:
+                n *= d
+            self.mem_size = n
+
+    def build(b0, nb):
+        raise AssertionError("no plan may be built for a refused batch")
+
+    monkeypatch.setenv("VDX_CONV2D_STREAMS", "2")
+    assert not F._image_groups(FakeBuf((4, 512, 257)), None, (), build)  # 4 images
+    assert not F._image_groups(FakeBuf((8, 64, 64)), None, (), build)  # 256 KiB
+    assert not F._image_groups(FakeBuf((512, 257)), None, (), build)  # not a batch
+    monkeypatch.setenv("VDX_CONV2D_STREAMS", "1")
+    assert not F._image_groups(FakeBuf((64, 512, 257)), None, (), build)
