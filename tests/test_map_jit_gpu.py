@@ -243,3 +243,25 @@ def test_compiled_plan_source_and_status_reset():
     assert rel_l2(dst.read(0), np.fft.fft(shifted_x, axis=1)) <= tol_fp32(16)
     plan = next(p for k, p in J._plans.items() if "(io + (long long)(1))" in k[-1])
     assert "vdx_mapped" in plan.source() and "FixPlan<16" in plan.source()
+
+
+def test_in_place_register_arithmetic():
+    """`op.register *= s` and `+=` assign the register (the reference's
+    in-place variable operators); a scalar added to the complex register adds
+    to both components, as on a vec2."""
+    rng = np.random.default_rng(71)
+    x = crandn(rng, (6, 360))
+    src = vd.asbuffer(x)
+    out = vd.Buffer((6, 360), vd.complex64)
+
+    @vd.map
+    def scaled_shift(buf: vc.Buffer[vc.c64], s: vc.Var[vc.f32]):
+        op = vd.fft.read_op()
+        op.read_from_buffer(buf)
+        op.register *= s
+        op.register += 0.5
+        op.register -= 0.25
+
+    vd.fft.fft(out, src, 1.5, input_map=scaled_shift)
+    ref = np.fft.fft(x.astype(np.complex128) * 1.5 + (0.25 + 0.25j), axis=1)
+    assert rel_l2(out.read(0), ref) <= tol_fp32(360)

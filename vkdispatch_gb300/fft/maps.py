@@ -73,6 +73,25 @@ class TraceRegister(vc.Sym):
     def __setitem__(self, key, value):
         self._events.append(("set", self._name, value))
 
+    # in-place arithmetic assigns the register, as the reference's variables
+    # do (vkdispatch/codegen/variables/variables.py:399-402); Python then
+    # rebinds the name to the register itself
+    def _assign(self, value):
+        self._events.append(("set", self._name, value))
+        return self
+
+    def __iadd__(self, other):
+        return self._assign(vc.Sym.__add__(self, other))
+
+    def __isub__(self, other):
+        return self._assign(vc.Sym.__sub__(self, other))
+
+    def __imul__(self, other):
+        return self._assign(vc.Sym.__mul__(self, other))
+
+    def __itruediv__(self, other):
+        return self._assign(vc.Sym.__truediv__(self, other))
+
     def conjugate(self):
         return vc.Sym("conj", vc.Sym("reg", self._name))
 

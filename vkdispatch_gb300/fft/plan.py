@@ -3,6 +3,7 @@ kernel factories, vkdispatch/fft/shader_factories.py:11, 107)."""
 
 from __future__ import annotations
 
+import collections
 import contextlib
 import ctypes
 import json
@@ -15,6 +16,7 @@ from .. import _lib as L
 
 _cache: Dict[tuple, "Plan"] = {}
 _mu = threading.Lock()
+_stats = [0, 0]  # plan-cache hits, misses
 _tls = threading.local()
 
 # storage types whose 16384-point C2C axes can run their short transforms on
@@ -164,11 +166,14 @@ def get_plan(
            kernel_op, kernel_type, bool(kernel_broadcast), int(flags))
     p = _cache.get(key)
     if p is not None:
+        _stats[0] += 1
         return p
     with _mu:
         p = _cache.get(key)
         if p is not None:
+            _stats[0] += 1
             return p
+        _stats[1] += 1
         d = L.FftDesc()
         d.ndim = len(shape)
         for i, s in enumerate(shape):
@@ -195,7 +200,14 @@ def get_plan(
 def cache_clear() -> None:
     with _mu:
         _cache.clear()
+        _stats[0] = _stats[1] = 0
 
 
-def cache_info() -> int:
-    return len(_cache)
+CacheInfo = collections.namedtuple("CacheInfo", ["hits", "misses", "maxsize", "currsize"])
+
+
+def cache_info() -> CacheInfo:
+    """Plan-cache counters in the form of functools' cache_info (the
+    reference reports its shader caches this way,
+    vkdispatch/fft/shader_factories.py:197-205); the cache is unbounded."""
+    return CacheInfo(_stats[0], _stats[1], None, len(_cache))
