@@ -67,3 +67,21 @@ def test_convolve_sweep(seed):
     x64 = x.astype(np.complex128)
     ref = np.fft.ifft(np.fft.fft(x64, axis=axis) * np.conj(k), axis=axis)
     assert rel_l2(b.read(0), ref) <= 3 * tol_fp32(shape[axis]), (shape, axis)
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_real_sweep(seed):
+    """rfft then irfft along the last axis: even lengths (half-length complex
+    FFT with the split) and odd ones (the full-length rule)."""
+    rng = np.random.default_rng(3000 + seed)
+    n = int(rng.choice([2, 6, 9, 16, 25, 100, 243, 512, 1000, 1001, 2187, 4096, 12005, 16384]))
+    rows = int(rng.choice([1, 3, 17]))
+    x = rng.standard_normal((rows, n)).astype(np.float32)
+    buf = vd.RFFTBuffer((rows, n))
+    buf.write_real(x)
+    vd.fft.rfft(buf)
+    spec = buf.read_fourier(0)
+    ref = np.fft.rfft(x.astype(np.float64), axis=-1)
+    assert rel_l2(spec, ref) <= 2 * tol_fp32(n), (rows, n)
+    vd.fft.irfft(buf)
+    assert rel_l2(buf.read_real(0), x) <= 4 * tol_fp32(n), (rows, n)
