@@ -173,3 +173,60 @@ def test_menu_refuses_real_store_of_an_expression():
     with pytest.raises(NotImplementedError):
         M.classify_output(power)
     assert M.classify_output(real_part).kind == "real"
+
+
+def test_control_flow_blocks_lower_and_compile():
+    """vc.if_block / else_if_block / else_block / while_block around traced
+    statements become the same C++ blocks in the hooks."""
+    import vkdispatch_gb300.codegen as vc2
+
+    buf = FakeBuffer((4, 10), vd.complex64)
+
+    @vd.map
+    def masked(b: vc2.Buffer[vc2.c64], lim: vc2.Var[vc2.i32]):
+        op = vd.fft.read_op()
+        op.read_from_buffer(b)
+        with vc2.if_block(vc2.any(op.fft_index >= lim, op.io_index < 3)):
+            op.register[:] = 0.0
+        with vc2.else_if_block(op.fft_index == 0):
+            op.register *= 2.0
+        with vc2.else_block():
+            n = vc2.new_register(vc2.i32, 0)
+            with vc2.while_block(n < 2):
+                op.register *= 1.5
+                n += 1
+
+    spec = J.build_hooks([buf], [buf, 4], [], masked, None, None, False)
+    src = spec.source
+    assert "if (" in src and "else if (" in src and "else {" in src and "while (" in src
+    assert src.count("{") == src.count("}")
+    _nvrtc_compile(spec.source, mode=0)
+
+
+def test_control_flow_misuse_is_refused():
+    import vkdispatch_gb300.codegen as vc2
+
+    buf = FakeBuffer((4, 10), vd.complex64)
+
+    @vd.map
+    def dangling_else(b: vc2.Buffer[vc2.c64]):
+        op = vd.fft.read_op()
+        op.read_from_buffer(b)
+        with vc2.else_block():
+            op.register *= 2.0
+
+    with pytest.raises(NotImplementedError):
+        J.build_hooks([buf], [buf], [], dangling_else, None, None, False)
+
+    @vd.map
+    def python_if(b: vc2.Buffer[vc2.c64]):
+        op = vd.fft.read_op()
+        op.read_from_buffer(b)
+        if op.fft_index < 3:  # a traced value has no Python truth value
+            op.register *= 2.0
+
+    with pytest.raises(NotImplementedError):
+        J.build_hooks([buf], [buf], [], python_if, None, None, False)
+    with pytest.raises(NotImplementedError):
+        with vc2.if_block(1):  # outside a traced map
+            pass

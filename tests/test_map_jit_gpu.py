@@ -265,3 +265,52 @@ def test_in_place_register_arithmetic():
     vd.fft.fft(out, src, 1.5, input_map=scaled_shift)
     ref = np.fft.fft(x.astype(np.complex128) * 1.5 + (0.25 + 0.25j), axis=1)
     assert rel_l2(out.read(0), ref) <= tol_fp32(360)
+
+
+def test_control_flow_maps():
+    """An input map that truncates the transform input past a length given
+    at call time (if_block), scales the first point (else_if_block) and runs
+    a counted loop (while_block); and an output map that writes two
+    different scalings by the output index (if / else)."""
+    rng = np.random.default_rng(72)
+    n, lim = 240, 150
+    x = crandn(rng, (5, n))
+    src = vd.asbuffer(x)
+    out = vd.Buffer((5, n), vd.complex64)
+
+    @vd.map
+    def truncate(buf: vc.Buffer[vc.c64], limit: vc.Var[vc.i32]):
+        op = vd.fft.read_op()
+        op.read_from_buffer(buf)
+        with vc.if_block(op.fft_index >= limit):
+            op.register[:] = 0.0
+        with vc.else_if_block(op.fft_index == 0):
+            op.register *= 3.0
+        with vc.else_block():
+            c = vc.new_register(vc.i32, 0)
+            with vc.while_block(c < 2):
+                op.register *= 2.0
+                c += 1
+
+    vd.fft.fft(out, src, lim, input_map=truncate)
+    y = x.astype(np.complex128) * 4.0
+    y[:, lim:] = 0.0
+    y[:, 0] = x[:, 0] * 3.0
+    ref = np.fft.fft(y, axis=1)
+    assert rel_l2(out.read(0), ref) <= tol_fp32(n)
+
+    dst = vd.Buffer((5, n), vd.complex64)
+
+    @vd.map
+    def split_scale(buf: vc.Buffer[vc.c64]):
+        op = vd.fft.write_op()
+        with vc.if_block(vc.all(op.fft_index > 0, op.fft_index < 10)):
+            buf[op.io_index] = op.register * 0.5
+        with vc.else_block():
+            buf[op.io_index] = op.register
+
+    b = vd.asbuffer(x)
+    vd.fft.fft(dst, b, output_map=split_scale)
+    ref = np.fft.fft(x.astype(np.complex128), axis=1)
+    ref[:, 1:10] *= 0.5
+    assert rel_l2(dst.read(0), ref) <= tol_fp32(n)

@@ -11,6 +11,8 @@ outside the menu raises NotImplementedError naming the function.
 
 from __future__ import annotations
 
+import contextlib
+
 from . import dtypes as dt
 
 f16, f32, f64 = dt.float16, dt.float32, dt.float64
@@ -43,6 +45,32 @@ class Sym:
     def __init__(self, op, *args):
         self.op = op
         self.args = args
+
+    # comparisons build traced conditions (for if_block and friends);
+    # == and != keep Python's identity meaning when Python itself asks
+    # (containers, `in`), so the equality overloads do not break lookups
+    __hash__ = object.__hash__
+
+    def __lt__(self, o):
+        return _Cmp("lt", self, o)
+
+    def __le__(self, o):
+        return _Cmp("le", self, o)
+
+    def __gt__(self, o):
+        return _Cmp("gt", self, o)
+
+    def __ge__(self, o):
+        return _Cmp("ge", self, o)
+
+    def __eq__(self, o):
+        return _Cmp("eq", self, o)
+
+    def __ne__(self, o):
+        return _Cmp("ne", self, o)
+
+    def __invert__(self):
+        return Sym("invert", self)
 
     def _bin(self, op, other):
         return Sym(op, self, other)
@@ -120,6 +148,19 @@ class Sym:
 
     def __repr__(self):
         return f"{self.op}({', '.join(map(repr, self.args))})"
+
+
+class _Cmp(Sym):
+    """A traced comparison.  As a Python bool, == and != mean identity;
+    ordering comparisons refuse, as the reference's variables do
+    (vkdispatch/codegen/variables/variables.py:338-339)."""
+
+    def __bool__(self):
+        if self.op == "eq":
+            return self.args[0] is self.args[1]
+        if self.op == "ne":
+            return self.args[0] is not self.args[1]
+        raise ValueError("traced values cannot be cast to a Python bool: use vc.if_block and friends")
 
 
 class SymBuffer:
@@ -264,6 +305,55 @@ def min(a, b):  # noqa: A001
 
 def max(a, b):  # noqa: A001
     return Sym("max", a, b)
+
+
+# --- control flow inside FFT maps (vkdispatch/codegen/functions/control_flow.py)
+# Each block is recorded as events around the statements traced inside it
+# and lowered to the same C++ block in the map's hook.
+@contextlib.contextmanager
+def if_block(cond):
+    from .fft import maps
+
+    maps.trace_control("if", cond)
+    yield
+    maps.trace_control("end")
+
+
+@contextlib.contextmanager
+def else_if_block(cond):
+    from .fft import maps
+
+    maps.trace_control("elif", cond)
+    yield
+    maps.trace_control("end")
+
+
+@contextlib.contextmanager
+def else_block():
+    from .fft import maps
+
+    maps.trace_control("else")
+    yield
+    maps.trace_control("end")
+
+
+@contextlib.contextmanager
+def while_block(cond):
+    from .fft import maps
+
+    maps.trace_control("while", cond)
+    yield
+    maps.trace_control("end")
+
+
+def any(*args):  # noqa: A001 - mirrors vc.any
+    """Logical or of traced conditions."""
+    return Sym("lor", *args)
+
+
+def all(*args):  # noqa: A001 - mirrors vc.all
+    """Logical and of traced conditions."""
+    return Sym("land", *args)
 
 
 # --- used by FFT map hooks (vkdispatch_gb300/fft/maps.py traces them) -------

@@ -20,8 +20,10 @@ arithmetic, vc.ravel_index / vc.unravel_index), scalar map arguments
 (vc.Var[...]), read_from_buffer / write_to_buffer with an io_index, register
 and component assignments, new_register temporaries, + - * / // % and
 unary minus, vc.mult_complex, conjugate(), to_dtype / to_complex and the
-math functions of vkdispatch_gb300.codegen.  Control flow (if_block and
-friends) is not traced and raises NotImplementedError.
+math functions of vkdispatch_gb300.codegen, and control flow: vc.if_block,
+else_if_block, else_block and while_block around traced statements, with
+conditions built from comparisons, vc.any / vc.all and integer ~ (lowered to
+the same C++ blocks; a value used as a condition is true when nonzero).
 """
 
 from __future__ import annotations
@@ -71,6 +73,9 @@ def phys_index(buf, ix: str) -> str:
         if d > 1 and st:
             terms.append(f"{c} * {st}LL")
     return "(" + (" + ".join(terms) or "0LL") + ")"
+
+
+_COMPARE = {"lt": "<", "le": "<=", "gt": ">", "ge": ">=", "eq": "==", "ne": "!="}
 
 
 def _wider(*kinds: str) -> str:
@@ -187,6 +192,19 @@ class _Lower:
             if "c" in (ka, kb):
                 self.fail("% on complex values")
             return f"vdx::mapops::m_mod({self.real(ca, ka)}, {self.real(cb, kb)})", "f"
+        if op in _COMPARE:
+            (ca, ka), (cb, kb) = self.expr(a[0]), self.expr(a[1])
+            if "c" in (ka, kb):
+                self.fail(f"a comparison ({op}) of complex values")
+            k = _wider(ka, kb)
+            return f"({self.as_kind(ca, ka, k)} {_COMPARE[op]} {self.as_kind(cb, kb, k)})", "i"
+        if op in ("lor", "land"):
+            return "(" + (" || " if op == "lor" else " && ").join(self.cond(x) for x in a) + ")", "i"
+        if op == "invert":
+            c, k = self.expr(a[0])
+            if k != "i":
+                self.fail("~ on a non-integer value")
+            return f"(~{c})", "i"
         if op in ("and", "or", "xor"):
             (ca, ka), (cb, kb) = self.expr(a[0]), self.expr(a[1])
             if ka != "i" or kb != "i":
@@ -318,11 +336,34 @@ class _Lower:
         return f"vdx::map_st<{ctype}>(m, {slot}, {ix}, ({ctype})({c}));"
 
     # ---- statements
+    def cond(self, e) -> str:
+        """A traced value used as a condition: nonzero is true."""
+        c, k = self.expr(e)
+        if k == "c":
+            self.fail("a complex value as a condition")
+        return f"({c} != {'0' if k == 'i' else 'Re(0)'})"
+
     def statements(self, events) -> List[str]:
         out = []
+        depth = 0
         for ev in events:
             kind = ev[0]
-            if kind == "new":
+            start = len(out)
+            if kind in ("if", "elif", "while"):
+                if kind == "elif" and not (out and out[-1].strip() == "}"):
+                    self.fail("else_if_block without an if_block right before it")
+                word = {"if": "if", "elif": "else if", "while": "while"}[kind]
+                out.append(f"{word} ({self.cond(ev[1])}) {{")
+                depth += 1
+            elif kind == "else":
+                if not (out and out[-1].strip() == "}"):
+                    self.fail("else_block without an if_block right before it")
+                out.append("else {")
+                depth += 1
+            elif kind == "end":
+                out.append("}")
+                depth -= 1
+            elif kind == "new":
                 _, name, var_type, init = ev
                 if getattr(var_type, "is_complex", False):
                     self.regs[name] = "c"
@@ -361,6 +402,12 @@ class _Lower:
                 out.append(self.store(i, idx, value))
             else:
                 self.fail(f"the event {kind}")
+            # statements inside blocks are indented by their depth
+            lead = "  " * (depth - (1 if kind in ("if", "elif", "while", "else") else 0))
+            if lead:
+                out[start:] = [lead + ln for ln in out[start:]]
+        if depth != 0:
+            self.fail("an unterminated control-flow block")
         return out
 
 

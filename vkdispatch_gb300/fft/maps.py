@@ -186,6 +186,15 @@ def write_op():
     return op
 
 
+def trace_control(kind: str, cond=None) -> None:
+    """Records the start ("if", "elif", "else", "while") or the end ("end")
+    of a control-flow block of the map being traced."""
+    events = getattr(_tls, "events", None)
+    if events is None:
+        raise NotImplementedError("control-flow blocks are traced only inside FFT map functions")
+    events.append((kind,) if cond is None else (kind, cond))
+
+
 def new_trace_register(var_type, *args):
     events = getattr(_tls, "events", None)
     if events is None:
@@ -225,9 +234,15 @@ def _has(expr, op, arg=None) -> bool:
     return any(_has(a, op, arg) for a in expr.args)
 
 
+_CONTROL = ("if", "elif", "else", "while", "end")
+
+
 def _menu_events(ev):
     """The events the menu matchers look at: new_register temporaries
-    declared without an initial value carry no operation of their own."""
+    declared without an initial value carry no operation of their own.  A map
+    with control flow is outside the menu (the map-hook compiler takes it)."""
+    if any(e[0] in _CONTROL for e in ev):
+        raise NotImplementedError("maps with control flow are outside the functor menu")
     return [e for e in ev if not (e[0] == "new" and not e[3])]
 
 
