@@ -44,6 +44,7 @@ extern "C" {
 #define VDX_F64 5
 #define VDX_I32 6
 #define VDX_U32 7
+#define VDX_V2F32 8 /* two float32 lanes (the reference's vec2): map-reduce results only */
 
 /* transform kinds */
 #define VDX_KIND_C2C 0  /* complex FFT along one axis, in or out of place */
@@ -386,6 +387,33 @@ int vdx_map_plan_destroy(vdx_map_plan* plan);
 int vdx_map_exec(const vdx_map_plan* plan, const vdx_map_args* args, void* stream);
 /* The full source NVRTC compiled for the plan (hooks and instantiation). */
 int vdx_map_plan_source(const vdx_map_plan* plan, char* buf, size_t n);
+
+/*
+ * Map-reduce with a compiled map: the reference's vd.reduce.map_reduce (and
+ * reduce(mapping_function=...)) with a mapping function outside vdx_reduce's
+ * fixed maps, e.g. one that reads several buffers or scalars
+ * (vkdispatch/reduce/stage.py:31-186, vkdispatch/reduce/reduce_function.py:
+ * 73-162).  hooks_source defines
+ *   struct VdxReduceHooks {
+ *     template <class Re> __device__ static auto map(const vdx::MapArgs& m, long long io);
+ *   };
+ * returning the element value for flat index io = row * n + i (a real,
+ * integer or vdx::Cx<Re> value; Cx lanes map to VDX_V2F32 components).
+ * out_type: VDX_F32, VDX_F64, VDX_I32, VDX_U32 or VDX_V2F32; op: VDX_RED_*
+ * (AND/OR/XOR only for VDX_I32 / VDX_U32).  Compiled with NVRTC at plan
+ * creation.  vdx_reduce_map_exec runs the same two stages as vdx_reduce:
+ * out[row] = op over i < n of map(row * n + i), with
+ * vdx_reduce_partial_count(n) partials per row in `workspace` (elements of
+ * out_type).  Map buffer indices outside their counts read 0 and set the
+ * plan's status (vdx_reduce_map_plan_status).
+ */
+typedef struct vdx_reduce_map_plan vdx_reduce_map_plan;
+int vdx_reduce_map_plan_create(const char* hooks_source, int op, int out_type, vdx_reduce_map_plan** plan);
+int vdx_reduce_map_plan_destroy(vdx_reduce_map_plan* plan);
+int vdx_reduce_map_exec(const vdx_reduce_map_plan* plan, const vdx_map_args* args, int64_t n, int64_t batch,
+                        void* out, void* workspace, void* stream);
+int vdx_reduce_map_plan_status(const vdx_reduce_map_plan* plan, int* status, int reset);
+int vdx_reduce_map_plan_source(const vdx_reduce_map_plan* plan, char* buf, size_t n);
 /* 1 when a launch of the plan indexed a map buffer out of range, else 0
  * (synchronous read; reset != 0 clears it). */
 int vdx_map_plan_status(const vdx_map_plan* plan, int* status, int reset);

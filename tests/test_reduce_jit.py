@@ -1,0 +1,88 @@
+"""CPU tests of compiled map-reduce (vkdispatch_gb300/reduce: _reduce_hooks ->
+csrc/reduce_mapped.cuh): maps outside vdx_reduce's fixed maps are traced and
+lowered to a VdxReduceHooks struct, and the generated source compiles with
+NVRTC against the two-stage reduction template.  No GPU is used."""
+
+import os
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import vkdispatch_gb300 as vd
+import vkdispatch_gb300.codegen as vc
+from vkdispatch_gb300.reduce import _reduce_hooks
+
+CSRC = Path(__file__).resolve().parent.parent / "vkdispatch_gb300" / "csrc"
+
+
+class FakeBuffer(vd.Buffer):
+    def __init__(self, shape, var_type):  # noqa: D107 - no device memory
+        self.shape, self.var_type, self.strides = tuple(shape), var_type, None
+        self.size = int(np.prod(shape))
+
+    @property
+    def ptr(self):
+        return 0
+
+
+def _compile(hooks, acc="float", re="float", op=0):
+    nvrtc = pytest.importorskip("cuda.bindings.nvrtc")
+    inc = os.environ.get("VDX_CUDA_INCLUDE") or os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"),
+                                                             "include")
+    if not os.path.exists(os.path.join(inc, "cuda_fp16.h")):
+        pytest.skip("CUDA headers not found")
+    src = ('#include "reduce_mapped.cuh"\n' + hooks +
+           f'\nextern "C" __global__ void vdx_mapped(vdx::MapArgs m, long long n, long long chunk, {acc}* part, '
+           f'int nparts) {{ vdx::reduce_mapped_partial<VdxReduceHooks, {re}, {acc}, {op}>(m, n, chunk, part, '
+           f'nparts); }}\n'
+           f'extern "C" __global__ void vdx_mapped_final(const {acc}* part, int nparts, {acc}* out) '
+           f'{{ vdx::reduce_mapped_final<{acc}, {op}>(part, nparts, out); }}\n')
+    err, prog = nvrtc.nvrtcCreateProgram(src.encode(), b"r.cu", 0, [], [])
+    opts = [b"--gpu-architecture=sm_103a", b"-std=c++17", f"-I{CSRC}".encode(), f"-I{inc}".encode(),
+            b"-default-device"]
+    (err,) = nvrtc.nvrtcCompileProgram(prog, len(opts), opts)
+    if err != nvrtc.nvrtcResult.NVRTC_SUCCESS:
+        _, size = nvrtc.nvrtcGetProgramLogSize(prog)
+        log = b" " * size
+        nvrtc.nvrtcGetProgramLog(prog, log)
+        pytest.fail(log.decode(errors="replace"))
+
+
+def test_listed_reduction_map_over_two_vec2_buffers():
+    """The reference's test_listed_reductions map: sin of the sum of two
+    vec2 buffers, reduced component-wise."""
+
+    def sum_map(buffer: vc.Buffer[vd.vec2], buffer2: vc.Buffer[vd.vec2]) -> vd.vec2:
+        ind = vd.reduce.mapped_io_index()
+        return vc.sin(buffer[ind] + buffer2[ind])
+
+    mf = vd.reduce.MappingFunction(sum_map)
+    a, b = FakeBuffer((1024,), vd.vec2), FakeBuffer((1024,), vd.vec2)
+    src, slots = _reduce_hooks(mf, (a, b))
+    assert "struct VdxReduceHooks" in src and "m_sin" in src and len(slots.buffers) == 2
+    _compile(src, acc="float2")
+
+
+def test_scalar_argument_and_integer_reduction():
+    def scaled(buf: vc.Buffer[vc.f32], s: vc.Var[vc.f32]) -> vc.f32:
+        return buf[vd.reduce.mapped_io_index()] * s + 1.0
+
+    src, slots = _reduce_hooks(vd.reduce.MappingFunction(scaled), (FakeBuffer((64,), vd.float32), 2.5))
+    assert "m.fs[0]" in src and slots.fscalars == [2.5]
+    _compile(src, acc="float", op=3)
+
+    def mixed(u: vc.Buffer[vc.u32]) -> vc.u32:
+        i = vd.reduce.mapped_io_index()
+        return u[i] ^ (i * 3)
+
+    src, _ = _reduce_hooks(vd.reduce.MappingFunction(mixed), (FakeBuffer((64,), vd.uint32),))
+    _compile(src, acc="unsigned", op=6)
+
+
+def test_argument_count_checked():
+    def one(buf: vc.Buffer[vc.f32]) -> vc.f32:
+        return buf[vd.reduce.mapped_io_index()]
+
+    with pytest.raises(ValueError):
+        _reduce_hooks(vd.reduce.MappingFunction(one), ())

@@ -36,7 +36,7 @@ NVCC_FLAGS = [
 ]
 
 # headers NVRTC compiles the map kernels from (csrc/jit.cu), in include order
-JIT_HEADERS = ("vdx_common.cuh", "fft_kernels.cuh", "fft_mapped.cuh")
+JIT_HEADERS = ("vdx_common.cuh", "fft_kernels.cuh", "fft_mapped.cuh", "reduce_mapped.cuh")
 
 
 def nvcc_path() -> str:

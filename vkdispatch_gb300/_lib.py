@@ -19,7 +19,7 @@ VDX_ERR_CUDA = 3
 VDX_ERR_NOMEM = 4
 
 # element types
-VDX_C64, VDX_C32, VDX_C128, VDX_BF16X2, VDX_F32, VDX_F64, VDX_I32, VDX_U32 = range(8)
+VDX_C64, VDX_C32, VDX_C128, VDX_BF16X2, VDX_F32, VDX_F64, VDX_I32, VDX_U32, VDX_V2F32 = range(9)
 
 
 def convert(src_ptr: int, src_type: int, dst_ptr: int, dst_type: int, count: int, stream: int) -> None:
@@ -63,6 +63,11 @@ EXPORTED = (
     "vdx_map_exec",
     "vdx_map_plan_source",
     "vdx_map_plan_status",
+    "vdx_reduce_map_plan_create",
+    "vdx_reduce_map_plan_destroy",
+    "vdx_reduce_map_exec",
+    "vdx_reduce_map_plan_status",
+    "vdx_reduce_map_plan_source",
 )
 VDX_REDUCE_NOALLOC_SCRATCH_BYTES = 1048576
 
@@ -185,6 +190,16 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.vdx_map_plan_source.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     lib.vdx_reduce_noalloc.restype = i32
     lib.vdx_reduce_noalloc.argtypes = [i32, i32, i32, vp, i64, i64, vp, vp]
+    lib.vdx_reduce_map_plan_create.restype = i32
+    lib.vdx_reduce_map_plan_create.argtypes = [ctypes.c_char_p, i32, i32, ctypes.POINTER(vp)]
+    lib.vdx_reduce_map_plan_destroy.restype = i32
+    lib.vdx_reduce_map_plan_destroy.argtypes = [vp]
+    lib.vdx_reduce_map_exec.restype = i32
+    lib.vdx_reduce_map_exec.argtypes = [vp, ctypes.POINTER(MapArgs), i64, i64, vp, vp, vp]
+    lib.vdx_reduce_map_plan_status.restype = i32
+    lib.vdx_reduce_map_plan_status.argtypes = [vp, ctypes.POINTER(ctypes.c_int), i32]
+    lib.vdx_reduce_map_plan_source.restype = i32
+    lib.vdx_reduce_map_plan_source.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
 
 
 def lib() -> ctypes.CDLL:

@@ -199,7 +199,12 @@ class _VarFactory:
 Var = _VarFactory()
 
 
-class _IoIndex:
+class _IoIndex(Sym):
+    """mapped_io_index() of a reduction map: the element's flat index."""
+
+    def __init__(self):
+        Sym.__init__(self, "io_index")
+
     def __repr__(self):
         return "io_index"
 

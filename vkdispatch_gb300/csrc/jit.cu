@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "fft_mapped.cuh"
+#include "reduce_mapped.cuh"
 #include "jit_headers.inc"  // kJitHeaderCount, kJitHeaderNames[], kJitHeaderSources[] (written by the build)
 #include "vdx.h"
 #include "vdx_internal.h"
@@ -268,6 +269,134 @@ int vdx_map_plan_status(const vdx_map_plan* p, int* status, int reset) {
 }
 
 int vdx_map_plan_source(const vdx_map_plan* p, char* buf, size_t n) {
+  if (!p || !buf || n == 0) return set_error(VDX_ERR_INVALID, "plan and a non-empty buffer are required");
+  std::snprintf(buf, n, "%s", p->source.c_str());
+  return p->source.size() < n ? VDX_OK : set_error(VDX_ERR_INVALID, "buffer too small for the source");
+}
+
+}  // extern "C"
+
+static_assert(VDX_RED_ADD == vdx::kRedAdd && VDX_RED_MUL == vdx::kRedMul && VDX_RED_MIN == vdx::kRedMin &&
+                  VDX_RED_MAX == vdx::kRedMax && VDX_RED_AND == vdx::kRedAnd && VDX_RED_OR == vdx::kRedOr &&
+                  VDX_RED_XOR == vdx::kRedXor,
+              "reduction op codes");
+
+struct vdx_reduce_map_plan {
+  int dev = 0;
+  int out_type = 0;
+  Module mod;
+  cudaKernel_t final_kernel = nullptr;
+  std::string source;
+  int* d_status = nullptr;
+  ~vdx_reduce_map_plan() {
+    if (d_status) cudaFree(d_status);
+  }
+};
+
+namespace {
+
+// accumulation type and register precision of a map-reduce output type
+bool reduce_types(int out_type, const char** acc, const char** re, size_t* bytes) {
+  switch (out_type) {
+    case VDX_F32: *acc = "float"; *re = "float"; *bytes = 4; return true;
+    case VDX_F64: *acc = "double"; *re = "double"; *bytes = 8; return true;
+    case VDX_I32: *acc = "int"; *re = "float"; *bytes = 4; return true;
+    case VDX_U32: *acc = "unsigned"; *re = "float"; *bytes = 4; return true;
+    case VDX_V2F32: *acc = "float2"; *re = "float"; *bytes = 8; return true;
+    default: return false;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int vdx_reduce_map_plan_create(const char* hooks_source, int op, int out_type, vdx_reduce_map_plan** plan) {
+  if (!hooks_source || !plan) return set_error(VDX_ERR_INVALID, "hooks_source and plan must be non-NULL");
+  *plan = nullptr;
+  const char *acc = nullptr, *re = nullptr;
+  size_t bytes = 0;
+  if (!reduce_types(out_type, &acc, &re, &bytes))
+    return set_error(VDX_ERR_INVALID, "out_type must be VDX_F32, VDX_F64, VDX_I32, VDX_U32 or VDX_V2F32");
+  if (op < VDX_RED_ADD || op > VDX_RED_XOR) return set_error(VDX_ERR_INVALID, "unknown reduction op");
+  if (op >= VDX_RED_AND && out_type != VDX_I32 && out_type != VDX_U32)
+    return set_error(VDX_ERR_INVALID, "AND / OR / XOR reductions need an integer output type");
+  auto* p = new vdx_reduce_map_plan();
+  cudaError_t e = cudaGetDevice(&p->dev);
+  if (e != cudaSuccess) {
+    delete p;
+    return set_error(VDX_ERR_CUDA, cudaGetErrorString(e));
+  }
+  p->out_type = out_type;
+  const std::string t = acc, r = re, o = std::to_string(op);
+  p->source = std::string("#include \"reduce_mapped.cuh\"\n\n") + hooks_source +
+              "\n\nextern \"C\" __global__ void __launch_bounds__(512) vdx_mapped(vdx::MapArgs m, long long n, "
+              "long long chunk, " + t + "* part, int nparts) {\n  vdx::reduce_mapped_partial<VdxReduceHooks, " + r +
+              ", " + t + ", " + o + ">(m, n, chunk, part, nparts);\n}\n\nextern \"C\" __global__ void "
+              "__launch_bounds__(512) vdx_mapped_final(const " + t + "* part, int nparts, " + t +
+              "* out) {\n  vdx::reduce_mapped_final<" + t + ", " + o + ">(part, nparts, out);\n}\n";
+  int rc = compile(p->source, p->dev, &p->mod);
+  if (rc != VDX_OK) {
+    delete p;
+    return rc;
+  }
+  e = cudaLibraryGetKernel(&p->final_kernel, p->mod.lib, "vdx_mapped_final");
+  if (e == cudaSuccess) e = cudaMalloc(&p->d_status, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, sizeof(int));
+  if (e != cudaSuccess) {
+    delete p;
+    return set_error(VDX_ERR_CUDA, (std::string("map-reduce plan: ") + cudaGetErrorString(e)).c_str());
+  }
+  *plan = p;
+  return VDX_OK;
+}
+
+int vdx_reduce_map_plan_destroy(vdx_reduce_map_plan* plan) {
+  delete plan;  // the compiled module stays cached for later plans of the same source
+  return VDX_OK;
+}
+
+int vdx_reduce_map_exec(const vdx_reduce_map_plan* p, const vdx_map_args* args, int64_t n, int64_t batch, void* out,
+                        void* workspace, void* stream) {
+  if (!p || !args || !out || !workspace) return set_error(VDX_ERR_INVALID, "plan, args, out and workspace are required");
+  if (n < 1 || batch < 1 || batch > 65535) return set_error(VDX_ERR_INVALID, "n >= 1 and 1 <= batch <= 65535 are required");
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != p->dev) return set_error(VDX_ERR_INVALID, "map-reduce plan was created on another device");
+  for (int i = 0; i < VDX_MAP_MAX_BUFFERS; ++i)
+    if (args->counts[i] < 0) return set_error(VDX_ERR_INVALID, "map buffer counts must be >= 0");
+  int64_t parts = 0;
+  int rc = vdx_reduce_partial_count(n, &parts);
+  if (rc != VDX_OK) return rc;
+  MapArgs m;
+  std::memcpy(&m, args, sizeof(vdx_map_args));
+  m.status = p->d_status;
+  long long nn = n, chunk = (n + parts - 1) / parts;
+  int np = (int)parts;
+  void* part = workspace;
+  void* a1[] = {&m, &nn, &chunk, &part, &np};
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(p->mod.kernel), dim3((unsigned)parts, (unsigned)batch),
+                                   dim3(512), a1, 0, s);
+  if (e == cudaSuccess) {
+    void* a2[] = {&part, &np, &out};
+    e = cudaLaunchKernel(reinterpret_cast<const void*>(p->final_kernel), dim3((unsigned)batch), dim3(512), a2, 0, s);
+  }
+  if (e != cudaSuccess) return set_error(VDX_ERR_CUDA, (std::string("map-reduce launch: ") + cudaGetErrorString(e)).c_str());
+  return VDX_OK;
+}
+
+int vdx_reduce_map_plan_status(const vdx_reduce_map_plan* p, int* status, int reset) {
+  if (!p || !status) return set_error(VDX_ERR_INVALID, "plan and status must be non-NULL");
+  int h = 0;
+  cudaError_t e = cudaMemcpy(&h, p->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && reset) e = cudaMemset(p->d_status, 0, sizeof(int));
+  if (e != cudaSuccess) return set_error(VDX_ERR_CUDA, cudaGetErrorString(e));
+  *status = h;
+  return VDX_OK;
+}
+
+int vdx_reduce_map_plan_source(const vdx_reduce_map_plan* p, char* buf, size_t n) {
   if (!p || !buf || n == 0) return set_error(VDX_ERR_INVALID, "plan and a non-empty buffer are required");
   std::snprintf(buf, n, "%s", p->source.c_str());
   return p->source.size() < n ? VDX_OK : set_error(VDX_ERR_INVALID, "buffer too small for the source");

@@ -49,6 +49,7 @@ _STORAGE = {
     dt.float64: ("double", "f"),
     dt.int32: ("int", "i"),
     dt.uint32: ("unsigned", "i"),
+    dt.vec2: ("vdx::Cx<float>", "c"),  # two float lanes, laid out as complex64
 }
 
 _UNARY = {"sin", "cos", "tan", "asin", "acos", "atan", "sinh", "cosh", "tanh", "exp", "exp2", "log", "log2", "sqrt",

@@ -172,6 +172,66 @@ def map(func=None, return_type=None, input_types=None):  # noqa: A001 - mirrors 
 _partial_counts: dict = {}  # n -> partial sums of the first stage (vdx_reduce_partial_count)
 
 
+_OUT_CODES = {dt.float32: L.VDX_F32, dt.float64: L.VDX_F64, dt.int32: L.VDX_I32, dt.uint32: L.VDX_U32,
+              dt.vec2: L.VDX_V2F32}
+
+
+class _CompiledReducePlan:
+    """A libvdx map-reduce plan whose map was compiled with NVRTC."""
+
+    def __init__(self, source: str, op: int, out_code: int):
+        h = ctypes.c_void_p()
+        L.check(L.lib().vdx_reduce_map_plan_create(source.encode(), op, out_code, ctypes.byref(h)), "map-reduce plan")
+        self.handle = h
+
+    def status(self, reset: bool = True) -> int:
+        c = ctypes.c_int()
+        L.check(L.lib().vdx_reduce_map_plan_status(self.handle, ctypes.byref(c), int(reset)), "map-reduce status")
+        return int(c.value)
+
+    def source(self) -> str:
+        buf = ctypes.create_string_buffer(1 << 16)
+        L.check(L.lib().vdx_reduce_map_plan_source(self.handle, buf, len(buf)), "map-reduce source")
+        return buf.value.decode()
+
+    def __del__(self):
+        try:
+            if self.handle:
+                L.lib().vdx_reduce_map_plan_destroy(self.handle)
+        except Exception:
+            pass
+
+
+_compiled_plans = {}  # (hooks source, op, output code, device) -> _CompiledReducePlan
+
+
+def _reduce_hooks(mf: "MappingFunction", args):
+    """Lowers a mapping function to the VdxReduceHooks struct that
+    vdx_reduce_map_plan_create compiles (csrc/reduce_mapped.cuh); returns the
+    source and the argument slots of this call."""
+    from ..fft import jit as J
+    from ..fft import maps as M
+
+    types = mf.input_dtypes()
+    flags = mf.arg_is_scalar()
+    if len(args) != len(types):
+        raise ValueError(f"map {mf.func.__name__} takes {len(types)} arguments, {len(args)} given")
+    syms = [M._TraceScalar(i, t) if sc else vc.SymBuffer(i, t) for i, (t, sc) in enumerate(zip(types, flags))]
+    try:
+        r = mf.func(*syms)
+    except NotImplementedError:
+        raise
+    except Exception as e:  # noqa: BLE001
+        raise NotImplementedError(f"map {mf.func.__name__} could not be traced: {e}") from e
+    slots = J.Slots()
+    low = J._Lower(mf.func.__name__, types, flags, list(args), slots)
+    code, _ = low.expr(r)
+    body = ["using namespace vdx::mapops;", "const long long k = 0, n = 0;", "(void)k; (void)n; (void)m;",
+            f"return {code};"]
+    src = "struct VdxReduceHooks {\n" + J._hook("auto map(const vdx::MapArgs& m, long long io)", body) + "};\n"
+    return src, slots
+
+
 class ReduceFunction:
     def __init__(self, reduction: ReduceOp, group_size: Optional[int] = None, axes: Optional[List[int]] = None,
                  mapping_function: Optional[MappingFunction] = None):
@@ -181,8 +241,87 @@ class ReduceFunction:
         self.map_func = mapping_function
         self.out_type = mapping_function.return_type if mapping_function is not None else None
         self._map_code = None
+        self._compiled_only = False  # the map is outside the fixed maps: always compiled
         # (input type, shape) -> validated launch layout of a call
         self._layouts = {}
+
+    def _needs_compiled_map(self, args) -> bool:
+        """Maps outside vdx_reduce's fixed maps (several arguments, other
+        expressions, other element types) run as a compiled map."""
+        if self.map_func is None:
+            return False
+        if self._compiled_only or len(args) != 1 or not isinstance(args[0], Buffer):
+            return True
+        t = args[0].var_type
+        if t.vdx_code is None or t.vdx_code in (L.VDX_C32, L.VDX_C128, L.VDX_BF16X2):
+            return True
+        try:
+            self._resolve_map(t)
+        except NotImplementedError:
+            self._compiled_only = True
+            return True
+        out_type = dt.float32 if t == dt.complex64 else t
+        return self.out_type is not None and self.out_type != out_type
+
+    def _rows(self, src):
+        """(n, batch): elements per reduced row and rows, from the axes."""
+        if self.axes is None:
+            return src.size, 1
+        shape = src.shape
+        batched = []
+        for i in range(len(shape)):
+            if i in self.axes:
+                break
+            batched.append(i)
+        skipped = []
+        for i in range(len(shape) - 1, -1, -1):
+            if i in self.axes:
+                break
+            skipped.append(i)
+        if skipped:
+            raise ValueError("Reduction axes must be contiguous!")
+        batch = int(np.prod([shape[i] for i in batched])) if batched else 1
+        return src.size // batch, batch
+
+    def _call_compiled(self, args, graph) -> Buffer:
+        import torch
+
+        from ..fft import jit as J
+
+        src = next((a for a in args if isinstance(a, Buffer)), None)
+        if src is None:
+            raise ValueError("a map-reduce needs at least one buffer argument")
+        out_type = self.out_type
+        if out_type not in _OUT_CODES:
+            raise NotImplementedError(f"map-reduce results of type {getattr(out_type, 'name', out_type)} "
+                                      "(float32, float64, int32, uint32 and vec2 are supported)")
+        op = self.reduction.code
+        if op >= L.VDX_RED_AND and out_type not in (dt.int32, dt.uint32):
+            raise ValueError(f"{self.reduction.name} reductions need an integer result type")
+        n, batch = self._rows(src)
+        source, slots = _reduce_hooks(self.map_func, args)
+        key = (source, op, _OUT_CODES[out_type], torch.cuda.current_device())
+        plan = _compiled_plans.get(key)
+        if plan is None:
+            plan = _compiled_plans[key] = _CompiledReducePlan(source, op, _OUT_CODES[out_type])
+        nparts = _partial_counts.get(n)
+        if nparts is None:
+            parts = ctypes.c_int64()
+            L.check(L.lib().vdx_reduce_partial_count(n, ctypes.byref(parts)), "reduce")
+            nparts = _partial_counts[n] = int(parts.value)
+        res = Buffer._empty((nparts + 1,) + ((batch,) if batch > 1 else ()), out_type)
+        margs = J.make_args(slots)
+        out = res.ptr
+        ws = out + batch * out_type.item_size
+        handle = plan.handle
+
+        def launch(stream):
+            L.check(L.lib().vdx_reduce_map_exec(handle, ctypes.byref(margs), n, batch, out, ws, stream),
+                    "map-reduce")
+
+        G.resolve(graph).record(launch, (plan, res, margs) + tuple(a for a in args if isinstance(a, Buffer)))
+        self.last_plan = plan
+        return res
 
     def _resolve_map(self, in_type: dt.dtype) -> int:
         if self.map_func is None:
@@ -192,6 +331,8 @@ class ReduceFunction:
         return self._map_code
 
     def __call__(self, *args, graph: Optional[G.CommandGraph] = None, **kwargs) -> Buffer:
+        if self._needs_compiled_map(args):
+            return self._call_compiled(args, graph)
         src = args[0]
         lay = self._layouts.get((src.var_type, src.shape))
         if lay is None:
