@@ -86,3 +86,23 @@ def test_argument_count_checked():
 
     with pytest.raises(ValueError):
         _reduce_hooks(vd.reduce.MappingFunction(one), ())
+
+
+def test_get_src_of_fixed_and_compiled_maps(capsys):
+    """ReduceFunction.get_src returns both stages (the reference's
+    test_min_max_codegen_stage_creation), for a fixed map and a compiled one."""
+
+    @vd.reduce.map_reduce(vd.reduce.SubgroupMin)
+    def min_map(buffer: vc.Buffer[vc.f32]) -> vc.f32:
+        return buffer[vd.reduce.mapped_io_index()]
+
+    @vd.reduce.map_reduce(vd.reduce.SubgroupMax)
+    def max_map(buffer: vc.Buffer[vc.f32], s: vc.Var[vc.f32]) -> vc.f32:
+        return buffer[vd.reduce.mapped_io_index()] * s
+
+    s1, s2 = min_map.get_src()
+    assert s1 and s2 and "k_reduce_partial" in s1.code
+    c1, c2 = max_map.get_src(line_numbers=True)
+    assert "VdxReduceHooks" in c1.code and "reduce_mapped_final" in c2.code
+    max_map.print_src()
+    assert "Reduction Stage 2" in capsys.readouterr().out

@@ -263,6 +263,49 @@ class ReduceFunction:
         out_type = dt.float32 if t == dt.complex64 else t
         return self.out_type is not None and self.out_type != out_type
 
+    def get_src(self, line_numbers: bool = None):
+        """The two stages as [stage 1, stage 2] sources (the reference's
+        ReduceFunction.get_src, vkdispatch/reduce/reduce_function.py:53-59):
+        the ahead-of-time kernels a fixed map runs on, or the compiled
+        map's hooks and instantiations."""
+        from ..fft.src_functions import ShaderSource, _numbered, _Placeholder
+
+        name = self.reduction.name
+        out_t = self.out_type
+        if self.map_func is None:
+            maps, compiled = "identity", False
+        else:
+            types = self.map_func.input_dtypes()
+            try:
+                if len(types) != 1:
+                    raise NotImplementedError("several arguments")
+                code = _trace_map(self.map_func.func, types)
+                maps = {L.VDX_MAP_IDENTITY: "identity", L.VDX_MAP_ABS: "abs", L.VDX_MAP_SQUARE: "square",
+                        L.VDX_MAP_REAL: "real", L.VDX_MAP_IMAG: "imag", L.VDX_MAP_SIN: "sin"}[code]
+                compiled = False
+            except NotImplementedError:
+                compiled = True
+        if not compiled:
+            s1 = (f"// stage 1: vdx::k_reduce_partial<In, T, {name}, {maps}> of libvdx.so (sm_103a):\n"
+                  "// grid (parts, rows) x 512 threads; each CTA folds one contiguous chunk of a row")
+            s2 = (f"// stage 2: vdx::k_reduce_final<T, {name}>: one CTA per row folds its partials in a fixed "
+                  "order")
+        else:
+            args = [0.0 if sc else _Placeholder(t) for t, sc in zip(self.map_func.input_dtypes(),
+                                                                    self.map_func.arg_is_scalar())]
+            hooks, _ = _reduce_hooks(self.map_func, args)
+            acc = {dt.float32: "float", dt.float64: "double", dt.int32: "int", dt.uint32: "unsigned",
+                   dt.vec2: "float2"}.get(out_t, "float")
+            s1 = ("// stage 1, compiled with NVRTC (csrc/reduce_mapped.cuh)\n" + hooks +
+                  f"// vdx::reduce_mapped_partial<VdxReduceHooks, Re, {acc}, {name}>")
+            s2 = f"// stage 2: vdx::reduce_mapped_final<{acc}, {name}>"
+        return [ShaderSource("reduction stage 1", _numbered(s1, bool(line_numbers)), (512, 1, 1)),
+                ShaderSource("reduction stage 2", _numbered(s2, bool(line_numbers)), (512, 1, 1))]
+
+    def print_src(self, line_numbers: bool = None):
+        srcs = self.get_src(line_numbers)
+        print(f"// Reduction Stage 1:\n{srcs[0]}\n// Reduction Stage 2:\n{srcs[1]}")
+
     def _rows(self, src):
         """(n, batch): elements per reduced row and rows, from the axes."""
         if self.axes is None:
