@@ -327,3 +327,13 @@ def test_image_groups_refuse_small_batches_without_gpu(monkeypatch):
     assert not F._image_groups(FakeBuf((512, 257)), None, (), build)  # not a batch
     monkeypatch.setenv("VDX_CONV2D_STREAMS", "1")
     assert not F._image_groups(FakeBuf((64, 512, 257)), None, (), build)
+
+
+def test_codegen_abbreviations_module():
+    """`from vkdispatch_gb300.codegen.abbreviations import *` gives the
+    reference's short names (vkdispatch/codegen/abbreviations.py)."""
+    ns = {}
+    exec("from vkdispatch_gb300.codegen.abbreviations import *", ns)
+    assert ns["f32"] is vd.float32 and ns["v2"] is vd.vec2 and ns["c64"] is vd.complex64
+    assert ns["Buff"][vd.float32].var_type is vd.float32
+    assert callable(vd.make_context) and callable(vd.get_context)

@@ -110,3 +110,22 @@ def test_strided_buffer_and_out_of_range_status():
     torch.cuda.synchronize()
     assert res.read(0)[0] == 999.0  # the out-of-range read loads 0
     assert shifted.last_plan.status() == 1
+
+
+def test_reference_preamble_and_abbreviations():
+    """The reference's test files start with vd.initialize and vd.make_context
+    and annotate maps with the abbreviations module: the same lines run here."""
+    from vkdispatch_gb300.codegen.abbreviations import Buff, f32
+
+    vd.initialize(debug_mode=True)
+    ctx = vd.make_context(use_cpu=True)
+    assert ctx.multiprocessor_count > 0 and vd.get_context() is ctx
+    data = np.random.default_rng(6).random(1536).astype(np.float32)
+    buf = vd.Buffer((1536,), vd.float32)
+    buf.write(data)
+
+    @vd.reduce.map_reduce(vd.reduce.SubgroupAdd)
+    def sum_map(buffer: Buff[f32]) -> f32:
+        return buffer[vd.reduce.mapped_io_index()]
+
+    assert np.allclose([data.sum()], [sum_map(buf).read(0)[0]])

@@ -43,6 +43,55 @@ from .reduce import MappingFunction, map  # noqa: F401
 
 __version__ = "0.1.0"
 
+# `from vkdispatch_gb300.codegen.abbreviations import *`, as user code writes
+# it for the reference (codegen is a module here, not a package)
+import sys as _sys  # noqa: E402
+
+from . import _abbreviations  # noqa: E402
+
+_sys.modules[__name__ + ".codegen.abbreviations"] = _abbreviations
+codegen.abbreviations = _abbreviations
+
+
+class Context:
+    """The device a process computes on (the reference's vd.Context,
+    made by vd.make_context): here the current CUDA device."""
+
+    def __init__(self, device: int):
+        import torch
+
+        self.device = device
+        props = torch.cuda.get_device_properties(device)
+        self.device_name = props.name
+        self.multiprocessor_count = props.multi_processor_count
+        self.total_memory = props.total_memory
+
+    def __repr__(self):
+        return f"Context(device={self.device}, {self.device_name})"
+
+
+_context = None
+
+
+def make_context(devices=None, use_cpu: bool = False, **kwargs) -> Context:
+    """Selects the GPU to compute on (the reference's vd.make_context,
+    which picks Vulkan or CUDA devices).  One CUDA device: `devices` may name
+    it (its first entry); `use_cpu` and the queue settings have no meaning
+    here and are accepted so that calls written for the reference run."""
+    import torch
+
+    global _context
+    if devices is not None:
+        dev = int(devices[0] if isinstance(devices, (list, tuple)) else devices)
+        torch.cuda.set_device(dev)
+    _load_lib()
+    _context = Context(torch.cuda.current_device())
+    return _context
+
+
+def get_context() -> Context:
+    return _context if _context is not None else make_context()
+
 
 def initialize(*args, **kwargs) -> None:
     """Loads libvdx (there is a single CUDA backend; arguments are ignored)."""
