@@ -10,6 +10,8 @@ Kernels live in libvdx.so (include/vdx.h), called through ctypes; PyTorch
 provides device memory and streams.  There is no CPU fallback.
 """
 
+import enum as _enum
+
 from . import codegen  # noqa: F401
 from . import fft  # noqa: F401
 from . import reduce  # noqa: F401
@@ -104,3 +106,17 @@ def is_cuda() -> bool:
 
 def get_backend() -> str:
     return "cuda"
+
+
+def is_vulkan() -> bool:
+    return False
+
+
+class LogLevel(_enum.IntEnum):
+    """Log levels vd.initialize(log_level=...) accepts (the reference's
+    vd.LogLevel); libvdx reports errors through exceptions and logs nothing."""
+
+    VERBOSE = 0
+    INFO = 1
+    WARNING = 2
+    ERROR = 3
