@@ -14,8 +14,6 @@ import os
 import threading
 from typing import Optional, Tuple, Union
 
-import numpy as np
-
 from .. import _lib as L
 from .. import dtypes as dt
 from .. import graph as G

@@ -28,7 +28,7 @@ from __future__ import annotations
 
 import threading
 from dataclasses import dataclass
-from typing import List, Optional
+from typing import Optional
 
 from .. import codegen as vc
 from .. import dtypes as dt
