@@ -417,7 +417,7 @@ def _run_ours(args):
 
 
 def summary(extra):
-    """The figures each extra workload is judged on, under short keys, so
+    """The headline figures of each extra workload, under short keys, so
     that the whole line fits the last few KB of the run's output (the full
     record, with the same figures under their long names, goes to stderr).
     Times in ms; frac = fraction of the measured HBM bandwidth."""
