@@ -117,3 +117,32 @@ def test_invalid_arguments():
         tf.fftn(x, s=(4,), dim=(0, 1))
     with pytest.raises(ValueError):
         tf.fft(x.cpu())
+
+
+@pytest.mark.parametrize("norm", [None, "forward", "ortho"])
+@pytest.mark.parametrize("n", [None, 30, 64])
+def test_hermitian_pair_and_shifts(norm, n):
+    """hfft / ihfft against torch.fft (values, and the hfft gradient in
+    FP64), fftshift / ifftshift and the frequency generators."""
+    g = torch.Generator(device="cuda").manual_seed(9)
+    h = torch.randn(4, 33, dtype=torch.complex64, device="cuda", generator=g)
+    got = tf.hfft(h, n=n, norm=norm)
+    ref = torch.fft.hfft(h, n=n, norm=norm)
+    assert got.shape == ref.shape
+    assert torch.linalg.norm(got - ref) <= 1e-5 * torch.linalg.norm(ref)
+    x = torch.randn(3, 48, dtype=torch.float32, device="cuda", generator=g)
+    got = tf.ihfft(x, n=n, norm=norm)
+    ref = torch.fft.ihfft(x, n=n, norm=norm)
+    assert got.shape == ref.shape
+    assert torch.linalg.norm(got - ref) <= 1e-5 * torch.linalg.norm(ref)
+    h64 = torch.randn(2, 17, dtype=torch.complex128, device="cuda", generator=g, requires_grad=True)
+    (tf.hfft(h64, n=n, norm=norm) ** 2).sum().backward()
+    ga = h64.grad.clone()
+    h64.grad = None
+    (torch.fft.hfft(h64, n=n, norm=norm) ** 2).sum().backward()
+    assert torch.allclose(ga, h64.grad, rtol=1e-9, atol=1e-9)
+    y = torch.randn(5, 6, 7, device="cuda", generator=g)
+    assert torch.equal(tf.fftshift(y), torch.fft.fftshift(y))
+    assert torch.equal(tf.ifftshift(y, dim=(0, 2)), torch.fft.ifftshift(y, dim=(0, 2)))
+    assert torch.equal(tf.fftshift(y, dim=1), torch.fft.fftshift(y, dim=1))
+    assert torch.equal(tf.fftfreq(10, 0.5), torch.fft.fftfreq(10, 0.5))

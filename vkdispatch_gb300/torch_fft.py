@@ -1,7 +1,7 @@
 """A torch.fft-compatible front end on libvdx kernels.
 
 `fft, ifft, rfft, irfft, fft2, ifft2, rfft2, irfft2, fftn, ifftn, rfftn,
-irfftn` take and return torch tensors with torch.fft's argument meanings:
+irfftn, hfft, ihfft` take and return torch tensors with torch.fft's argument meanings:
 `n` / `s` zero-pad or trim the transformed dimensions, `dim` picks them and
 `norm` is "backward" (default: forward unscaled, inverse 1/n), "forward"
 (forward 1/n, inverse unscaled) or "ortho" (1/sqrt(n) both ways).  Results
@@ -10,8 +10,11 @@ are new tensors; gradients flow through the hand-written adjoints of
 contiguous first) but must live on the GPU: there is no CPU path.  Real
 inputs of the complex transforms are promoted to complex64 (float32 and
 narrower) or complex128 (float64).  Lengths with prime factors above 13 run
-as Bluestein transforms (up to 8192 points in complex64, 4096 in
-complex128); their real transforms go through the complex ones.
+as Bluestein transforms (up to 2^23 points in complex64, 4096 in
+complex128); their real transforms go through the complex ones.  `hfft` /
+`ihfft` are the Hermitian pair (irfft / rfft of the conjugate with the
+opposite normalisation), `fftshift` / `ifftshift` roll the dimensions, and
+`fftfreq` / `rfftfreq` are torch's own generators.
 
 The reference's own interop is the contiguous CAI buffer
 (vkdispatch/base/buffer.py:353-362); this module is the torch-side entry to
@@ -209,4 +212,51 @@ def irfft2(input, s=None, dim=(-2, -1), norm=None):
     return irfftn(input, s, dim, norm)
 
 
-__all__ = ["fft", "ifft", "rfft", "irfft", "fft2", "ifft2", "rfft2", "irfft2", "fftn", "ifftn", "rfftn", "irfftn"]
+# ---------------------------------------------------------------------------
+# Hermitian transforms, shifts and sample frequencies
+# ---------------------------------------------------------------------------
+_SWAP = {None: "forward", "backward": "forward", "forward": "backward", "ortho": "ortho"}
+
+
+def _swap(norm: Optional[str]) -> str:
+    if norm not in _SWAP:
+        raise ValueError(f'norm must be one of "backward", "forward", "ortho" (got {norm!r})')
+    return _SWAP[norm]
+
+
+def hfft(input: torch.Tensor, n: Optional[int] = None, dim: int = -1, norm: Optional[str] = None) -> torch.Tensor:
+    """The one-sided half of a Hermitian signal to its real spectrum:
+    irfft of the conjugate with the opposite normalisation (torch.fft.hfft)."""
+    return irfft(_complex(_cuda(input)).conj(), n=n, dim=dim, norm=_swap(norm))
+
+
+def ihfft(input: torch.Tensor, n: Optional[int] = None, dim: int = -1, norm: Optional[str] = None) -> torch.Tensor:
+    """A real signal to the one-sided half of its Hermitian inverse
+    spectrum: the conjugate of rfft with the opposite normalisation
+    (torch.fft.ihfft)."""
+    return rfft(input, n=n, dim=dim, norm=_swap(norm)).conj()
+
+
+def _shift_dims(x: torch.Tensor, dim):
+    if dim is None:
+        return tuple(range(x.dim()))
+    return (dim,) if isinstance(dim, int) else tuple(dim)
+
+
+def fftshift(input: torch.Tensor, dim=None) -> torch.Tensor:
+    """Moves the zero-frequency bin to the centre (torch.fft.fftshift)."""
+    dims = _shift_dims(input, dim)
+    return torch.roll(input, shifts=[input.shape[d] // 2 for d in dims], dims=dims)
+
+
+def ifftshift(input: torch.Tensor, dim=None) -> torch.Tensor:
+    """The inverse of fftshift (torch.fft.ifftshift)."""
+    dims = _shift_dims(input, dim)
+    return torch.roll(input, shifts=[-(input.shape[d] // 2) for d in dims], dims=dims)
+
+
+fftfreq = torch.fft.fftfreq  # sample frequencies: tensor generators, no transform
+rfftfreq = torch.fft.rfftfreq
+
+__all__ = ["fft", "ifft", "rfft", "irfft", "fft2", "ifft2", "rfft2", "irfft2", "fftn", "ifftn", "rfftn", "irfftn",
+           "hfft", "ihfft", "fftshift", "ifftshift", "fftfreq", "rfftfreq"]
