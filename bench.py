@@ -372,8 +372,8 @@ def _run_ours(args):
                 "parallelism": "replicas" if world > 1 else "single GPU",
                 "error_rel_l2_vs_fp64": err,
                 "per_kernel_ms": {k: round(v, 5) for k, v in mean_k.items()},
-                "step": f"vd.fft.convolve2DR: {nparts} groups of {B // nparts} images, each group's "
-                        "rfft -> conv -> irfft on its own stream",
+                "step": f"vd.fft.convolve2DR -> vdx_conv2d_groups_exec: {nparts} groups of {B // nparts} "
+                        "images, each group's rfft -> conv -> irfft on its own stream",
                 "kernel_ms_from": "second pass: the three kernels over all 64 images on one stream, "
                                   "events between kernels",
                 "wall_s_timed_region": round(wall, 4),

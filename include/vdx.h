@@ -214,6 +214,29 @@ int vdx_fft_exec_ops(const vdx_plan* plan, const void* in, void* out, const void
 int vdx_conv_exec_multi(const vdx_plan* plan, const void* in, void* out, const void* kernel, int kernel_num,
                         int64_t kernel_stride, int64_t out_stride, void* stream);
 
+/*
+ * convolve2DR of a batch of real images as image groups (the reference's
+ * vd.fft.convolve2DR, vkdispatch/fft/functions.py:614-646, which the
+ * reference runs as rfft -> convolve(axis 1) -> irfft over the whole batch).
+ * desc: VDX_KIND_CONV2D_REAL, ndim 3, REAL shape (B, H, W) with W even,
+ * axis 1, io_type = compute_type = VDX_C64, normalize as in
+ * VDX_KIND_CONV2D_REAL, kernel_broadcast 1 = one (H, W/2+1) kernel spectrum
+ * for every image; flags 0 or VDX_FFT_FLAG_AUTOTUNE.  The images are cut
+ * into `groups` (1..8, at most B) runs; each run's three transforms go on a
+ * stream the plan owns, forked from and joined back into the caller's stream
+ * with events, so that the groups' latency-bound kernels overlap.  Results
+ * equal those of one group.  vdx_conv2d_groups_exec runs in place on the
+ * packed RFFT layout (data), enqueues only asynchronous work (capturable in a
+ * CUDA graph) and must not be called on one plan from two host threads at
+ * once.
+ */
+typedef struct vdx_conv2d_groups_plan vdx_conv2d_groups_plan;
+
+int vdx_conv2d_groups_plan_create(const vdx_fft_desc* desc, int groups, vdx_conv2d_groups_plan** plan);
+int vdx_conv2d_groups_plan_destroy(vdx_conv2d_groups_plan* plan);
+int vdx_conv2d_groups_plan_describe(const vdx_conv2d_groups_plan* plan, char* buf, size_t n);
+int vdx_conv2d_groups_exec(const vdx_conv2d_groups_plan* plan, void* data, const void* kernel, void* stream);
+
 /* Number of CTAs one vdx_fft_exec of this plan launches. */
 int vdx_fft_plan_ctas(const vdx_plan* plan, int64_t* ctas);
 

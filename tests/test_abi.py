@@ -125,3 +125,37 @@ def test_multi_kernel_and_batch_validation_without_gpu():
     assert lib.vdx_batch_plan_create(None, 0, 0, 1, None) == L.VDX_ERR_INVALID
     ws = ctypes.c_size_t()
     assert lib.vdx_batch_workspace_bytes(None, ctypes.byref(ws)) == L.VDX_ERR_INVALID
+
+
+def _conv2d_groups_desc(shape=(8, 64, 64)):
+    d = L.FftDesc()
+    d.ndim = 3
+    for i, x in enumerate(shape):
+        d.shape[i] = x
+    d.axis = 1
+    d.kind = L.VDX_KIND_CONV2D_REAL
+    d.normalize = 1
+    d.io_type = d.compute_type = L.VDX_C64
+    d.signal_lo = d.signal_hi = -1
+    return d
+
+
+@pytest.mark.parametrize(
+    "field,value,groups",
+    [("kind", 3, 2), ("ndim", 2, 2), ("axis", 2, 2), ("io_type", 2, 2), ("flags", 1, 2), (None, None, 0),
+     (None, None, 9), ("shape", (8, 64, 63), 2), ("shape", (0, 64, 64), 2)],
+)
+def test_conv2d_groups_validation_without_gpu(field, value, groups):
+    """vdx_conv2d_groups_plan_create checks the descriptor and group count
+    before any CUDA call and leaves the handle NULL."""
+    d = _conv2d_groups_desc(value if field == "shape" else (8, 64, 64))
+    if field not in (None, "shape"):
+        setattr(d, field, value)
+    h = ctypes.c_void_p()
+    rc = L.lib().vdx_conv2d_groups_plan_create(ctypes.byref(d), groups, ctypes.byref(h))
+    assert rc in (L.VDX_ERR_INVALID, L.VDX_ERR_UNSUPPORTED), L.last_error()
+    assert not h.value
+    lib = L.lib()
+    assert lib.vdx_conv2d_groups_exec(None, None, None, None) == L.VDX_ERR_INVALID
+    assert lib.vdx_conv2d_groups_plan_describe(None, None, 0) == L.VDX_ERR_INVALID
+    assert lib.vdx_conv2d_groups_plan_destroy(None) == L.VDX_OK

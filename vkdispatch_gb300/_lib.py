@@ -68,6 +68,10 @@ EXPORTED = (
     "vdx_reduce_map_exec",
     "vdx_reduce_map_plan_status",
     "vdx_reduce_map_plan_source",
+    "vdx_conv2d_groups_plan_create",
+    "vdx_conv2d_groups_plan_destroy",
+    "vdx_conv2d_groups_plan_describe",
+    "vdx_conv2d_groups_exec",
 )
 VDX_REDUCE_NOALLOC_SCRATCH_BYTES = 1048576
 
@@ -164,6 +168,14 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.vdx_convert.argtypes = [vp, i32, vp, i32, i64, vp]
     lib.vdx_conv_exec_multi.restype = i32
     lib.vdx_conv_exec_multi.argtypes = [vp, vp, vp, vp, i32, i64, i64, vp]
+    lib.vdx_conv2d_groups_plan_create.restype = i32
+    lib.vdx_conv2d_groups_plan_create.argtypes = [ctypes.POINTER(FftDesc), i32, ctypes.POINTER(vp)]
+    lib.vdx_conv2d_groups_plan_destroy.restype = i32
+    lib.vdx_conv2d_groups_plan_destroy.argtypes = [vp]
+    lib.vdx_conv2d_groups_plan_describe.restype = i32
+    lib.vdx_conv2d_groups_plan_describe.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+    lib.vdx_conv2d_groups_exec.restype = i32
+    lib.vdx_conv2d_groups_exec.argtypes = [vp, vp, vp, vp]
     lib.vdx_batch_plan_create.restype = i32
     lib.vdx_batch_plan_create.argtypes = [ctypes.POINTER(BatchItem), i32, i32, i32, ctypes.POINTER(vp)]
     lib.vdx_batch_plan_destroy.restype = i32

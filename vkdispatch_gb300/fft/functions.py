@@ -921,9 +921,12 @@ def _groupable(*buffers) -> bool:
 
 def _conv2d_split(buffer, kernel, kernel_inner_only, normalize, graph, print_shader) -> bool:
     """convolve2DR as image groups: rfft rows -> column convolution -> irfft
-    rows per group (see _image_groups)."""
+    rows per group, on the streams of one vdx_conv2d_groups plan (the C call
+    that forks, runs and joins the groups; same size rules as _image_groups)."""
     real_shape = tuple(int(x) for x in buffer.real_shape)
-    if len(real_shape) != 3:
+    parts = _conv2d_split_parts()
+    if (len(real_shape) != 3 or parts < 2 or real_shape[0] < 8 or buffer.mem_size < (16 << 20)
+            or real_shape[2] % 2):
         return False
     img = math.prod(buffer.shape[1:])  # complex elements per image
     broadcast = bool(kernel_inner_only)
@@ -931,19 +934,16 @@ def _conv2d_split(buffer, kernel, kernel_inner_only, normalize, graph, print_sha
         if kernel.size < img:
             raise ValueError(f"kernel buffer of {kernel.size} elements is smaller than the signal ({buffer.size})")
         broadcast = True
+    plan = P.get_conv2d_groups_plan(real_shape, min(parts, real_shape[0] // 4), bool(normalize), broadcast)
+    if print_shader:
+        print(plan.describe())
+    data, ker = buffer.ptr, kernel.ptr
 
-    def build(b0, nb):
-        rs = (nb,) + real_shape[1:]
-        fs = (nb,) + tuple(int(x) for x in buffer.shape[1:])
-        ptr = buffer.ptr + b0 * img * 8
-        kptr = kernel.ptr if broadcast else kernel.ptr + b0 * img * 8
-        return [(P.get_plan(rs, 2, L.VDX_KIND_R2C, False, False, L.VDX_C64, L.VDX_C64, None), ptr, ptr, None),
-                (P.get_plan(fs, 1, L.VDX_KIND_CONV, False, bool(normalize), L.VDX_C64, L.VDX_C64, None,
-                            L.VDX_KOP_MUL_CONJ, L.VDX_C64, broadcast), ptr, ptr, kptr),
-                (P.get_plan(rs, 2, L.VDX_KIND_C2R, True, bool(normalize), L.VDX_C64, L.VDX_C64, None), ptr, ptr,
-                 None)]
+    def launch(s):
+        plan.exec(data, ker, s)
 
-    return _image_groups(buffer, graph, (buffer, kernel), build, print_shader)
+    _record(graph, launch, (buffer, kernel, plan))
+    return True
 
 
 def _axes_split(buffer, steps, graph, print_shader) -> bool:

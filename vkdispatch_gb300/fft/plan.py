@@ -197,10 +197,73 @@ def get_plan(
         return p
 
 
+class Conv2DGroupsPlan:
+    """vdx_conv2d_groups_plan: convolve2DR of a (B, H, W) batch of real images
+    as image groups on streams the plan owns (one C call per execution)."""
+
+    def __init__(self, real_shape: Tuple[int, int, int], groups: int, normalize: bool, broadcast: bool,
+                 flags: int):
+        d = L.FftDesc()
+        d.ndim = 3
+        for i, s in enumerate(real_shape):
+            d.shape[i] = int(s)
+        d.axis = 1
+        d.kind = L.VDX_KIND_CONV2D_REAL
+        d.normalize = int(bool(normalize))
+        d.io_type = d.compute_type = L.VDX_C64
+        d.signal_lo = d.signal_hi = -1
+        d.kernel_op = L.VDX_KOP_MUL_CONJ
+        d.kernel_type = L.VDX_C64
+        d.kernel_broadcast = int(bool(broadcast))
+        d.flags = int(flags)
+        self.desc = d
+        h = ctypes.c_void_p()
+        L.check(L.lib().vdx_conv2d_groups_plan_create(ctypes.byref(d), int(groups), ctypes.byref(h)),
+                "image-group convolve2DR plan")
+        self.handle = h
+
+    def describe(self) -> dict:
+        buf = ctypes.create_string_buffer(1024)
+        L.check(L.lib().vdx_conv2d_groups_plan_describe(self.handle, buf, len(buf)), "image-group plan describe")
+        return json.loads(buf.value.decode())
+
+    def exec(self, data_ptr: int, ker_ptr: int, stream: int) -> None:
+        L.check(L.lib().vdx_conv2d_groups_exec(self.handle, data_ptr, ker_ptr, stream), "image-group convolve2DR")
+
+    def __del__(self):
+        try:
+            if self.handle:
+                L.lib().vdx_conv2d_groups_plan_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def get_conv2d_groups_plan(real_shape: Tuple[int, int, int], groups: int, normalize: bool,
+                           broadcast: bool) -> Conv2DGroupsPlan:
+    """The calling thread's image-group plan for these arguments: a plan's
+    streams and events serve one host thread at a time, so each thread keeps
+    its own plans."""
+    flags = L.VDX_FFT_FLAG_AUTOTUNE if getattr(_tls, "tune", False) else 0
+    key = (torch.cuda.current_device(), tuple(int(x) for x in real_shape), int(groups), bool(normalize),
+           bool(broadcast), flags)
+    cache = getattr(_tls, "groups", None)
+    if cache is None:
+        cache = _tls.groups = {}
+    p = cache.get(key)
+    if p is None:
+        _stats[1] += 1
+        p = cache[key] = Conv2DGroupsPlan(real_shape, groups, normalize, broadcast, flags)
+    else:
+        _stats[0] += 1
+    return p
+
+
 def cache_clear() -> None:
     with _mu:
         _cache.clear()
         _stats[0] = _stats[1] = 0
+    if getattr(_tls, "groups", None):
+        _tls.groups.clear()
 
 
 CacheInfo = collections.namedtuple("CacheInfo", ["hits", "misses", "maxsize", "currsize"])
