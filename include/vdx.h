@@ -237,6 +237,28 @@ int vdx_conv2d_groups_plan_destroy(vdx_conv2d_groups_plan* plan);
 int vdx_conv2d_groups_plan_describe(const vdx_conv2d_groups_plan* plan, char* buf, size_t n);
 int vdx_conv2d_groups_exec(const vdx_conv2d_groups_plan* plan, void* data, const void* kernel, void* stream);
 
+/*
+ * The same image groups for any chain of 1-4 in-place per-image transforms
+ * of one batch (the reference's fft2 / ifft2 / rfft2 / irfft2 / convolve2D,
+ * vkdispatch/fft/functions.py:164-300, 373-448, 549-612, each of which it runs as one
+ * launch per transform over the whole batch).  steps[s] describes transform
+ * s over the WHOLE batch: ndim 3, shape[0] = the image count (the same in
+ * every step), axis 1 or 2, VDX_KIND_C2C, R2C, C2R or CONV, complex64
+ * storage and compute, and every step addresses the same bytes per image
+ * (R2C / C2R steps take the real shape and the packed RFFT layout).  The plan
+ * cuts the batch into `groups` (1..8) runs of images, each with its own plans
+ * and stream.  vdx_group_exec runs the chain in place on data; a CONV step
+ * reads `kernel` at the image's offset (or at kernel itself when the step
+ * has kernel_broadcast = 1).  Same stream, capture and threading rules as
+ * vdx_conv2d_groups_exec.
+ */
+typedef struct vdx_group_plan vdx_group_plan;
+
+int vdx_group_plan_create(const vdx_fft_desc* steps, int nsteps, int groups, vdx_group_plan** plan);
+int vdx_group_plan_destroy(vdx_group_plan* plan);
+int vdx_group_plan_describe(const vdx_group_plan* plan, char* buf, size_t n);
+int vdx_group_exec(const vdx_group_plan* plan, void* data, const void* kernel, void* stream);
+
 /* Number of CTAs one vdx_fft_exec of this plan launches. */
 int vdx_fft_plan_ctas(const vdx_plan* plan, int64_t* ctas);
 

@@ -159,3 +159,42 @@ def test_conv2d_groups_validation_without_gpu(field, value, groups):
     assert lib.vdx_conv2d_groups_exec(None, None, None, None) == L.VDX_ERR_INVALID
     assert lib.vdx_conv2d_groups_plan_describe(None, None, 0) == L.VDX_ERR_INVALID
     assert lib.vdx_conv2d_groups_plan_destroy(None) == L.VDX_OK
+
+
+def _group_steps(specs):
+    arr = (L.FftDesc * len(specs))()
+    for d, (shape, axis, kind) in zip(arr, specs):
+        d.ndim = len(shape)
+        for i, x in enumerate(shape):
+            d.shape[i] = x
+        d.axis = axis
+        d.kind = kind
+        d.io_type = d.compute_type = L.VDX_C64
+        d.signal_lo = d.signal_hi = -1
+    return arr
+
+
+@pytest.mark.parametrize(
+    "specs,groups",
+    [
+        ([], 2),  # no steps
+        ([((8, 64, 64), 1, L.VDX_KIND_C2C)] * 5, 2),  # more than 4 steps
+        ([((8, 64, 64), 1, L.VDX_KIND_C2C)], 0),  # group count
+        ([((8, 64, 64), 0, L.VDX_KIND_C2C)], 2),  # axis 0 runs across images
+        ([((8, 64, 64), 1, L.VDX_KIND_CONV2D_REAL)], 2),  # not a per-image step
+        ([((8, 64, 64), 2, L.VDX_KIND_R2C), ((8, 64, 64), 1, L.VDX_KIND_C2C)], 2),  # 33 vs 64 columns
+        ([((8, 64, 64), 1, L.VDX_KIND_C2C), ((4, 64, 64), 2, L.VDX_KIND_C2C)], 2),  # image counts differ
+        ([((8, 64, 63), 2, L.VDX_KIND_R2C)], 2),  # odd real width
+        ([((64, 64), 1, L.VDX_KIND_C2C)], 2),  # not a batch of images
+    ],
+)
+def test_group_plan_validation_without_gpu(specs, groups):
+    """vdx_group_plan_create refuses malformed chains before any CUDA call."""
+    arr = _group_steps(specs) if specs else None
+    h = ctypes.c_void_p()
+    rc = L.lib().vdx_group_plan_create(arr, len(specs), groups, ctypes.byref(h))
+    assert rc == L.VDX_ERR_INVALID, L.last_error()
+    assert not h.value
+    assert L.lib().vdx_group_exec(None, None, None, None) == L.VDX_ERR_INVALID
+    assert L.lib().vdx_group_plan_describe(None, None, 0) == L.VDX_ERR_INVALID
+    assert L.lib().vdx_group_plan_destroy(None) == L.VDX_OK

@@ -1,8 +1,9 @@
-"""vdx_conv2d_groups_plan through the C ABI alone (ctypes on include/vdx.h,
-no Python FFT layer): the image groups' rfft -> column convolution -> irfft
-chains on the plan's own streams give the FP64 result, the same result as
-one group, for uneven groups, broadcast kernels, non-square images and
-CUDA-graph capture of the caller's stream."""
+"""vdx_conv2d_groups_plan and vdx_group_plan through the C ABI alone
+(ctypes on include/vdx.h, no Python FFT layer): the image groups' chains of
+transforms on the plans' own streams give the FP64 result, the same result
+as one group, for uneven groups, broadcast kernels, non-square images,
+four-step rows, CUDA-graph capture of the caller's stream, and the fft2 /
+ifft2 / rfft2 / convolve2D chains."""
 
 import ctypes
 import json
@@ -151,3 +152,93 @@ def test_odd_width_refused_on_device():
     h = ctypes.c_void_p()
     assert L.lib().vdx_conv2d_groups_plan_create(ctypes.byref(d), 2, ctypes.byref(h)) == L.VDX_ERR_INVALID
     assert not h.value
+
+
+def _steps(specs):
+    arr = (L.FftDesc * len(specs))()
+    for d, (shape, axis, kind, inverse, normalize, broadcast) in zip(arr, specs):
+        d.ndim = 3
+        for i, x in enumerate(shape):
+            d.shape[i] = x
+        d.axis, d.kind, d.inverse, d.normalize = axis, kind, int(inverse), int(normalize)
+        d.io_type = d.compute_type = L.VDX_C64
+        d.signal_lo = d.signal_hi = -1
+        d.kernel_op = L.VDX_KOP_MUL_CONJ
+        d.kernel_type = L.VDX_C64
+        d.kernel_broadcast = int(broadcast)
+    return arr
+
+
+class _Chain:
+    def __init__(self, specs, groups):
+        self.h = ctypes.c_void_p()
+        arr = _steps(specs)
+        L.check(L.lib().vdx_group_plan_create(arr, len(specs), groups, ctypes.byref(self.h)), "create")
+
+    def describe(self):
+        buf = ctypes.create_string_buffer(1024)
+        L.check(L.lib().vdx_group_plan_describe(self.h, buf, len(buf)), "describe")
+        return json.loads(buf.value.decode())
+
+    def exec(self, data, ker=None):
+        L.check(L.lib().vdx_group_exec(self.h, data.data_ptr(), None if ker is None else ker.data_ptr(),
+                                       torch.cuda.current_stream().cuda_stream), "exec")
+
+    def __del__(self):
+        L.lib().vdx_group_plan_destroy(self.h)
+
+
+def _crand(rng, shape):
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+
+
+@pytest.mark.parametrize("n,H,W,groups", [(8, 256, 512, 2), (11, 128, 384, 3), (8, 64, 16384, 2)])
+def test_group_chain_fft2_ifft2(n, H, W, groups):
+    """fft2 then ifft2 as two chains; the 16384-point rows are four-step plans
+    with a workspace per group."""
+    rng = np.random.default_rng(n + W)
+    x = _crand(rng, (n, H, W))
+    data = torch.from_numpy(x).cuda()
+    C2C = L.VDX_KIND_C2C
+    fwd = _Chain([((n, H, W), 1, C2C, 0, 0, 0), ((n, H, W), 2, C2C, 0, 0, 0)], groups)
+    inv = _Chain([((n, H, W), 1, C2C, 1, 1, 0), ((n, H, W), 2, C2C, 1, 1, 0)], groups)
+    assert fwd.describe()["group_images"] == [n * (g + 1) // groups - n * g // groups for g in range(groups)]
+    fwd.exec(data)
+    torch.cuda.synchronize()
+    assert rel_l2(data.cpu().numpy(), np.fft.fft2(x.astype(np.complex128))) <= 2 * tol_fp32(H, W)
+    inv.exec(data)
+    torch.cuda.synchronize()
+    assert rel_l2(data.cpu().numpy(), x) <= 4 * tol_fp32(H, W)
+
+
+def test_group_chain_rfft2_and_convolve2d():
+    rng = np.random.default_rng(5)
+    n, H, W = 9, 256, 256
+    x = rng.uniform(-1, 1, (n, H, W)).astype(np.float32)
+    data = _packed(x)
+    R = (n, H, W)
+    HC = W // 2 + 1
+    rfft2 = _Chain([(R, 2, L.VDX_KIND_R2C, 0, 0, 0), ((n, H, HC), 1, L.VDX_KIND_C2C, 0, 0, 0)], 2)
+    rfft2.exec(data)
+    torch.cuda.synchronize()
+    assert rel_l2(data.cpu().numpy(), np.fft.rfft2(x.astype(np.float64))) <= 2 * tol_fp32(H, W)
+    # convolve2D of a complex batch with one broadcast kernel spectrum
+    z = _crand(rng, (n, H, W))
+    K = _crand(rng, (H, W)) * 0.05
+    zt = torch.from_numpy(z).cuda()
+    conv = _Chain([((n, H, W), 2, L.VDX_KIND_C2C, 0, 0, 0), ((n, H, W), 1, L.VDX_KIND_CONV, 0, 1, 1),
+                   ((n, H, W), 2, L.VDX_KIND_C2C, 1, 1, 0)], 3)
+    conv.exec(zt, torch.from_numpy(K).cuda())
+    torch.cuda.synchronize()
+    z64 = z.astype(np.complex128)
+    S = np.fft.fft(z64, axis=2)
+    ref = np.fft.ifft(np.fft.ifft(np.fft.fft(S, axis=1) * np.conj(K), axis=1), axis=2)
+    assert rel_l2(zt.cpu().numpy(), ref) <= 4 * tol_fp32(H, W)
+
+
+def test_group_chain_needs_kernel_for_convolution():
+    n, H, W = 8, 64, 64
+    conv = _Chain([((n, H, W), 1, L.VDX_KIND_CONV, 0, 1, 0)], 2)
+    data = torch.zeros((n, H, W), dtype=torch.complex64, device="cuda")
+    rc = L.lib().vdx_group_exec(conv.h, data.data_ptr(), None, torch.cuda.current_stream().cuda_stream)
+    assert rc == L.VDX_ERR_INVALID and "kernel" in L.last_error()

@@ -1,6 +1,6 @@
 """convolve2DR over a batch of images split into groups, each group's
 rfft -> convolution -> irfft chain on its own stream (fft/functions.py
-_conv2d_split): the same results as one group on the caller's stream, for
+_conv2d_split, through vdx_group_plan): the same results as one group on the caller's stream, for
 replicated and broadcast kernels, uneven groups, CUDA-graph capture and
 deferred CommandGraph recording."""
 
@@ -149,7 +149,8 @@ def test_fft2_ifft2_and_convolve2d_groups(parts, monkeypatch):
 
 def test_long_axes_keep_one_group(monkeypatch):
     """Axes of 8192 points and up plan as four-step pairs that own a
-    workspace: those chains stay on the caller's stream."""
+    workspace; each image group has its own plans, so those chains split
+    too."""
     rng = np.random.default_rng(40)
     x = _crand(rng, (8, 64, 16384))
     buf = vd.asbuffer(x)

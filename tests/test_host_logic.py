@@ -318,15 +318,17 @@ def test_image_groups_refuse_small_batches_without_gpu(monkeypatch):
                 n *= d
             self.mem_size = n
 
-    def build(b0, nb):
+    def no_plan(*a, **k):
         raise AssertionError("no plan may be built for a refused batch")
 
+    monkeypatch.setattr(F.P, "get_group_plan", no_plan)
+    steps = [((4, 512, 257), 2, 0, False, False, False)]
     monkeypatch.setenv("VDX_CONV2D_STREAMS", "2")
-    assert not F._image_groups(FakeBuf((4, 512, 257)), None, (), build)  # 4 images
-    assert not F._image_groups(FakeBuf((8, 64, 64)), None, (), build)  # 256 KiB
-    assert not F._image_groups(FakeBuf((512, 257)), None, (), build)  # not a batch
+    assert not F._image_groups(FakeBuf((4, 512, 257)), None, (), steps)  # 4 images
+    assert not F._image_groups(FakeBuf((8, 64, 64)), None, (), steps)  # 256 KiB
+    assert not F._image_groups(FakeBuf((512, 257)), None, (), steps)  # not a batch
     monkeypatch.setenv("VDX_CONV2D_STREAMS", "1")
-    assert not F._image_groups(FakeBuf((64, 512, 257)), None, (), build)
+    assert not F._image_groups(FakeBuf((64, 512, 257)), None, (), steps)
 
 
 def test_codegen_abbreviations_module():

@@ -72,6 +72,10 @@ EXPORTED = (
     "vdx_conv2d_groups_plan_destroy",
     "vdx_conv2d_groups_plan_describe",
     "vdx_conv2d_groups_exec",
+    "vdx_group_plan_create",
+    "vdx_group_plan_destroy",
+    "vdx_group_plan_describe",
+    "vdx_group_exec",
 )
 VDX_REDUCE_NOALLOC_SCRATCH_BYTES = 1048576
 
@@ -176,6 +180,14 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.vdx_conv2d_groups_plan_describe.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     lib.vdx_conv2d_groups_exec.restype = i32
     lib.vdx_conv2d_groups_exec.argtypes = [vp, vp, vp, vp]
+    lib.vdx_group_plan_create.restype = i32
+    lib.vdx_group_plan_create.argtypes = [ctypes.POINTER(FftDesc), i32, i32, ctypes.POINTER(vp)]
+    lib.vdx_group_plan_destroy.restype = i32
+    lib.vdx_group_plan_destroy.argtypes = [vp]
+    lib.vdx_group_plan_describe.restype = i32
+    lib.vdx_group_plan_describe.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+    lib.vdx_group_exec.restype = i32
+    lib.vdx_group_exec.argtypes = [vp, vp, vp, vp]
     lib.vdx_batch_plan_create.restype = i32
     lib.vdx_batch_plan_create.argtypes = [ctypes.POINTER(BatchItem), i32, i32, i32, ctypes.POINTER(vp)]
     lib.vdx_batch_plan_destroy.restype = i32

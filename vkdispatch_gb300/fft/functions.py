@@ -11,7 +11,6 @@ from __future__ import annotations
 
 import math
 import os
-import threading
 from typing import Optional, Tuple, Union
 
 from .. import _lib as L
@@ -764,25 +763,12 @@ def convolve2D(buffer: Buffer, kernel: Buffer, kernel_map=None, buffer_shape=Non
             and output_map is None and output_type in (None, dt.complex64) and input_type in (None, dt.complex64)
             and kernel_type in (None, dt.complex64) and compute_type in (None, dt.complex64)
             and _groupable(buffer, kernel) and len(buffer.shape) == 3):
-        img = math.prod(buffer.shape[1:])
-        broadcast = bool(kernel_inner_only)
-        if not broadcast and kernel.size < buffer.size:
-            if kernel.size < img:
-                raise ValueError(f"kernel buffer of {kernel.size} elements is smaller than the signal "
-                                 f"({buffer.size})")
-            broadcast = True
-
-        def build(b0, nb):
-            shape = (nb,) + tuple(int(x) for x in buffer.shape[1:])
-            ptr = buffer.ptr + b0 * img * 8
-            kptr = kernel.ptr if broadcast else kernel.ptr + b0 * img * 8
-            return [(P.get_plan(shape, 2, L.VDX_KIND_C2C, False, False, L.VDX_C64, L.VDX_C64, None), ptr, ptr, None),
-                    (P.get_plan(shape, 1, L.VDX_KIND_CONV, False, bool(normalize), L.VDX_C64, L.VDX_C64, None,
-                                L.VDX_KOP_MUL_CONJ, L.VDX_C64, broadcast), ptr, ptr, kptr),
-                    (P.get_plan(shape, 2, L.VDX_KIND_C2C, True, bool(normalize), L.VDX_C64, L.VDX_C64, None), ptr,
-                     ptr, None)]
-
-        if _image_groups(buffer, graph, (buffer, kernel), build, print_shader):
+        broadcast = _kernel_broadcast(buffer, kernel, kernel_inner_only)
+        shape = tuple(int(x) for x in buffer.shape)
+        steps = [(shape, 2, L.VDX_KIND_C2C, False, False, False),
+                 (shape, 1, L.VDX_KIND_CONV, False, bool(normalize), broadcast),
+                 (shape, 2, L.VDX_KIND_C2C, True, bool(normalize), False)]
+        if _image_groups(buffer, graph, (buffer, kernel), steps, print_shader, kernel):
             return
     fft(buffer, graph=graph, print_shader=print_shader, input_map=input_map, output_type=output_type,
         input_type=input_type, compute_type=compute_type)
@@ -833,12 +819,6 @@ def _conv2d_fused(buffer, kernel, kernel_inner_only, normalize, graph, print_sha
     return True
 
 
-# per host thread: (device, parts) -> (side streams, fork event, join events).
-# The fork and join events are re-recorded by every call, so two host
-# threads must not share them.
-_split_tls = threading.local()
-
-
 def _conv2d_split_parts() -> int:
     """How many image groups a batched convolve2DR runs as, each on its own
     stream (VDX_CONV2D_STREAMS, default 2; 1 = one group on the caller's
@@ -849,69 +829,35 @@ def _conv2d_split_parts() -> int:
         return 2
 
 
-def _image_groups(buffer, graph, keep, build, print_shader=False) -> bool:
+def _image_groups(buffer, graph, keep, steps, print_shader=False, kernel=None) -> bool:
     """Runs a batch of 2-D images as `parts` groups of images, each group's
-    chain of launches on its own library-owned stream, forked from and
-    joined back into the caller's stream.  Every kernel of such a chain is
-    latency-bound at partial occupancy, so one group's kernels fill the SMs
-    that another group's kernel leaves idle while it drains (convolve2DR of
-    64 x 512^2 on GB300: 0.0954 ms for two groups of 32 against 0.1019 ms for
-    one group of 64).  Each image goes through the same plans' arithmetic, so
-    the results are those of one group.
+    chain of launches on its own plan-owned stream, forked from and joined
+    back into the caller's stream (vdx_group_plan, one C call per execution).
+    Every kernel of such a chain is latency-bound at partial occupancy, so one
+    group's kernels fill the SMs that another group's kernel leaves idle while
+    it drains (convolve2DR of 64 x 512^2 on GB300: 0.0944 ms for two groups of
+    32 against 0.1019 ms for one group of 64).  Each image goes through the
+    same arithmetic, so the results are those of one group.
 
-    build(b0, nb) returns the plans of images [b0, b0 + nb) as a list of
-    (plan, in_ptr, out_ptr, ker_ptr).  Returns False (nothing recorded) for a
-    buffer that is not a batch of at least 8 images of 16 MiB or more in all,
-    or with VDX_CONV2D_STREAMS=1."""
-    import torch
-
+    steps: (shape, axis, kind, inverse, normalize, kernel_broadcast) of each
+    transform over the whole batch, in place on `buffer`; a CONV step reads
+    `kernel`.  Returns False (nothing recorded) for a buffer that is not a
+    batch of at least 8 images of 16 MiB or more in all, or with
+    VDX_CONV2D_STREAMS=1."""
     parts = _conv2d_split_parts()
     if parts < 2 or len(buffer.shape) != 3 or int(buffer.shape[0]) < 8 or buffer.mem_size < (16 << 20):
         return False
-    nimg = int(buffer.shape[0])
-    parts = min(parts, nimg // 4)
-    cut = [nimg * i // parts for i in range(parts + 1)]
-    groups = [build(cut[i], cut[i + 1] - cut[i]) for i in range(parts)]
-    # groups of equal size share plans, and a plan that owns a workspace
-    # (four-step and Bluestein axes) must not run on two streams at once
-    if any(_owns_workspace(pl) for g in groups for pl, *_ in g):
-        return False
+    plan = P.get_group_plan(tuple(steps), min(parts, int(buffer.shape[0]) // 4))
     if print_shader:
-        for g in groups:
-            print(*(pl.describe() for pl, *_ in g))
-    dev = torch_device_index()
-    cache = getattr(_split_tls, "streams", None)
-    if cache is None:
-        cache = _split_tls.streams = {}
-    st = cache.get((dev, parts))
-    if st is None:
-        st = ([torch.cuda.Stream(device=dev) for _ in range(parts)], torch.cuda.Event(),
-              [torch.cuda.Event() for _ in range(parts)])
-        cache[(dev, parts)] = st
-    sides, fork, joins = st
-    handles = [int(x.cuda_stream) for x in sides]
+        print(plan.describe())
+    data = buffer.ptr
+    ker = kernel.ptr if kernel is not None else None
 
     def launch(s):
-        caller = torch.cuda.ExternalStream(s) if s else torch.cuda.current_stream()
-        fork.record(caller)
-        for side, h, join, g in zip(sides, handles, joins, groups):
-            side.wait_event(fork)
-            for pl, src, dst, ker in g:
-                pl.exec(src, dst, ker, h)
-            join.record(side)
-            caller.wait_event(join)
+        plan.exec(data, ker, s)
 
-    _record(graph, launch, keep)
+    _record(graph, launch, tuple(keep) + (plan,))
     return True
-
-
-def _owns_workspace(plan) -> bool:
-    ws = getattr(plan, "_owns_workspace", None)
-    if ws is None:
-        d = plan.describe()
-        ws = "fourstep" in d or "bluestein" in d
-        plan._owns_workspace = ws
-    return ws
 
 
 def _groupable(*buffers) -> bool:
@@ -919,47 +865,39 @@ def _groupable(*buffers) -> bool:
     return all(b.var_type == dt.complex64 and b.contiguous for b in buffers)
 
 
+def _kernel_broadcast(buffer, kernel, kernel_inner_only) -> bool:
+    """Whether one kernel spectrum serves every image: kernel_inner_only, or a
+    kernel buffer of one image (smaller buffers are refused)."""
+    if kernel_inner_only or kernel.size >= buffer.size:
+        return bool(kernel_inner_only)
+    img = math.prod(buffer.shape[1:])
+    if kernel.size < img:
+        raise ValueError(f"kernel buffer of {kernel.size} elements is smaller than the signal ({buffer.size})")
+    return True
+
+
 def _conv2d_split(buffer, kernel, kernel_inner_only, normalize, graph, print_shader) -> bool:
     """convolve2DR as image groups: rfft rows -> column convolution -> irfft
-    rows per group, on the streams of one vdx_conv2d_groups plan (the C call
-    that forks, runs and joins the groups; same size rules as _image_groups)."""
+    rows per group (see _image_groups)."""
     real_shape = tuple(int(x) for x in buffer.real_shape)
-    parts = _conv2d_split_parts()
-    if (len(real_shape) != 3 or parts < 2 or real_shape[0] < 8 or buffer.mem_size < (16 << 20)
-            or real_shape[2] % 2):
+    if len(real_shape) != 3 or real_shape[2] % 2:
         return False
-    img = math.prod(buffer.shape[1:])  # complex elements per image
-    broadcast = bool(kernel_inner_only)
-    if not broadcast and kernel.size < buffer.size:
-        if kernel.size < img:
-            raise ValueError(f"kernel buffer of {kernel.size} elements is smaller than the signal ({buffer.size})")
-        broadcast = True
-    plan = P.get_conv2d_groups_plan(real_shape, min(parts, real_shape[0] // 4), bool(normalize), broadcast)
-    if print_shader:
-        print(plan.describe())
-    data, ker = buffer.ptr, kernel.ptr
-
-    def launch(s):
-        plan.exec(data, ker, s)
-
-    _record(graph, launch, (buffer, kernel, plan))
-    return True
+    broadcast = _kernel_broadcast(buffer, kernel, kernel_inner_only)
+    shape = tuple(int(x) for x in buffer.shape)
+    steps = [(real_shape, 2, L.VDX_KIND_R2C, False, False, False),
+             (shape, 1, L.VDX_KIND_CONV, False, bool(normalize), broadcast),
+             (real_shape, 2, L.VDX_KIND_C2R, True, bool(normalize), False)]
+    return _image_groups(buffer, graph, (buffer, kernel), steps, print_shader, kernel)
 
 
 def _axes_split(buffer, steps, graph, print_shader) -> bool:
     """A chain of per-image transforms of a (batch, H, W) buffer as image
     groups; steps = [(kind, axis, inverse, normalize, real_shape_or_None)]."""
-    img = math.prod(buffer.shape[1:])
-
-    def build(b0, nb):
-        ptr = buffer.ptr + b0 * img * 8
-        out = []
-        for kind, ax, inv, norm, real in steps:
-            shape = (nb,) + tuple(int(x) for x in (real if real is not None else buffer.shape)[1:])
-            out.append((P.get_plan(shape, ax, kind, inv, norm, L.VDX_C64, L.VDX_C64, None), ptr, ptr, None))
-        return out
-
-    return _image_groups(buffer, graph, (buffer,), build, print_shader)
+    if any(real is not None and int(real[-1]) % 2 for *_, real in steps):
+        return False
+    full = [(tuple(int(x) for x in (real if real is not None else buffer.shape)), ax, kind, inv, norm, False)
+            for kind, ax, inv, norm, real in steps]
+    return _image_groups(buffer, graph, (buffer,), full, print_shader)
 
 
 def torch_device_index() -> int:

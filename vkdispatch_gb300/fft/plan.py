@@ -138,6 +138,20 @@ class Plan:
             pass
 
 
+def _default_flags(shape, axis: int, kind: int, io_type: int, compute_type: int, signal_range) -> int:
+    """Plan flags from the calling thread's settings (tensor-core stages,
+    autotuning, Bluestein)."""
+    flags = 0
+    if (getattr(_tls, "tc", False) and kind == L.VDX_KIND_C2C and int(shape[axis]) == 16384
+            and io_type in _TC_IO and compute_type == L.VDX_C64 and signal_range is None):
+        flags = L.VDX_FFT_FLAG_TENSOR_CORE
+    if getattr(_tls, "tune", False):
+        flags |= L.VDX_FFT_FLAG_AUTOTUNE
+    if bluestein_enabled() and kind == L.VDX_KIND_C2C:
+        flags |= L.VDX_FFT_FLAG_BLUESTEIN
+    return flags
+
+
 def get_plan(
     shape: Tuple[int, ...],
     axis: int,
@@ -154,14 +168,7 @@ def get_plan(
 ) -> Plan:
     dev = torch.cuda.current_device()
     if flags is None:
-        flags = 0
-        if (getattr(_tls, "tc", False) and kind == L.VDX_KIND_C2C and int(shape[axis]) == 16384
-                and io_type in _TC_IO and compute_type == L.VDX_C64 and signal_range is None):
-            flags = L.VDX_FFT_FLAG_TENSOR_CORE
-        if getattr(_tls, "tune", False):
-            flags |= L.VDX_FFT_FLAG_AUTOTUNE
-        if bluestein_enabled() and kind == L.VDX_KIND_C2C:
-            flags |= L.VDX_FFT_FLAG_BLUESTEIN
+        flags = _default_flags(shape, axis, kind, io_type, compute_type, signal_range)
     key = (dev, tuple(shape), axis, kind, bool(inverse), int(normalize), io_type, compute_type, signal_range,
            kernel_op, kernel_type, bool(kernel_broadcast), int(flags))
     p = _cache.get(key)
@@ -197,62 +204,62 @@ def get_plan(
         return p
 
 
-class Conv2DGroupsPlan:
-    """vdx_conv2d_groups_plan: convolve2DR of a (B, H, W) batch of real images
-    as image groups on streams the plan owns (one C call per execution)."""
+class GroupPlan:
+    """vdx_group_plan: a chain of in-place per-image transforms of a
+    (B, H, W) batch, cut into image groups on streams the plan owns (one C
+    call per execution forks, runs and joins the groups)."""
 
-    def __init__(self, real_shape: Tuple[int, int, int], groups: int, normalize: bool, broadcast: bool,
-                 flags: int):
-        d = L.FftDesc()
-        d.ndim = 3
-        for i, s in enumerate(real_shape):
-            d.shape[i] = int(s)
-        d.axis = 1
-        d.kind = L.VDX_KIND_CONV2D_REAL
-        d.normalize = int(bool(normalize))
-        d.io_type = d.compute_type = L.VDX_C64
-        d.signal_lo = d.signal_hi = -1
-        d.kernel_op = L.VDX_KOP_MUL_CONJ
-        d.kernel_type = L.VDX_C64
-        d.kernel_broadcast = int(bool(broadcast))
-        d.flags = int(flags)
-        self.desc = d
+    def __init__(self, steps: Tuple[tuple, ...], groups: int):
+        arr = (L.FftDesc * len(steps))()
+        for d, (shape, axis, kind, inverse, normalize, broadcast) in zip(arr, steps):
+            d.ndim = len(shape)
+            for i, x in enumerate(shape):
+                d.shape[i] = int(x)
+            d.axis = axis
+            d.kind = kind
+            d.inverse = int(bool(inverse))
+            d.normalize = int(normalize)
+            d.io_type = d.compute_type = L.VDX_C64
+            d.signal_lo = d.signal_hi = -1
+            d.kernel_op = L.VDX_KOP_MUL_CONJ
+            d.kernel_type = L.VDX_C64
+            d.kernel_broadcast = int(bool(broadcast))
+            d.flags = _default_flags(shape, axis, kind, L.VDX_C64, L.VDX_C64, None)
+        self.steps = arr
         h = ctypes.c_void_p()
-        L.check(L.lib().vdx_conv2d_groups_plan_create(ctypes.byref(d), int(groups), ctypes.byref(h)),
-                "image-group convolve2DR plan")
+        L.check(L.lib().vdx_group_plan_create(arr, len(steps), int(groups), ctypes.byref(h)), "image-group plan")
         self.handle = h
 
     def describe(self) -> dict:
         buf = ctypes.create_string_buffer(1024)
-        L.check(L.lib().vdx_conv2d_groups_plan_describe(self.handle, buf, len(buf)), "image-group plan describe")
+        L.check(L.lib().vdx_group_plan_describe(self.handle, buf, len(buf)), "image-group plan describe")
         return json.loads(buf.value.decode())
 
-    def exec(self, data_ptr: int, ker_ptr: int, stream: int) -> None:
-        L.check(L.lib().vdx_conv2d_groups_exec(self.handle, data_ptr, ker_ptr, stream), "image-group convolve2DR")
+    def exec(self, data_ptr: int, ker_ptr: Optional[int], stream: int) -> None:
+        L.check(L.lib().vdx_group_exec(self.handle, data_ptr, ker_ptr, stream), "image-group exec")
 
     def __del__(self):
         try:
             if self.handle:
-                L.lib().vdx_conv2d_groups_plan_destroy(self.handle)
+                L.lib().vdx_group_plan_destroy(self.handle)
         except Exception:
             pass
 
 
-def get_conv2d_groups_plan(real_shape: Tuple[int, int, int], groups: int, normalize: bool,
-                           broadcast: bool) -> Conv2DGroupsPlan:
-    """The calling thread's image-group plan for these arguments: a plan's
-    streams and events serve one host thread at a time, so each thread keeps
-    its own plans."""
-    flags = L.VDX_FFT_FLAG_AUTOTUNE if getattr(_tls, "tune", False) else 0
-    key = (torch.cuda.current_device(), tuple(int(x) for x in real_shape), int(groups), bool(normalize),
-           bool(broadcast), flags)
+def get_group_plan(steps: Tuple[tuple, ...], groups: int) -> GroupPlan:
+    """The calling thread's image-group plan for this chain of steps
+    ((shape, axis, kind, inverse, normalize, kernel_broadcast) each): a
+    plan's streams and events serve one host thread at a time, so each
+    thread keeps its own plans."""
+    key = (torch.cuda.current_device(), tuple(steps), int(groups),
+           tuple(_default_flags(st[0], st[1], st[2], L.VDX_C64, L.VDX_C64, None) for st in steps))
     cache = getattr(_tls, "groups", None)
     if cache is None:
         cache = _tls.groups = {}
     p = cache.get(key)
     if p is None:
         _stats[1] += 1
-        p = cache[key] = Conv2DGroupsPlan(real_shape, groups, normalize, broadcast, flags)
+        p = cache[key] = GroupPlan(tuple(steps), groups)
     else:
         _stats[0] += 1
     return p
