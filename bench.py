@@ -340,11 +340,17 @@ def _run_ours(args):
     e2e_steps(max(3, args.warmup))
     torch.cuda.synchronize()
     KE = max(8, K // 2)
-    e2e_ms = max_over_ranks(e2e_time(KE), dist)
-    last = h_out[(KE - 1) % NBUF][..., :W].numpy()
-    e2e_err = float(np.linalg.norm((last - ref).ravel()) / np.linalg.norm(ref.ravel()))
-    e2e_steps(3, transform=False)
-    copy_ms = max_over_ranks(e2e_time(KE, transform=False), dist)
+    # three rounds, each the full loop then the copies alone, so that a
+    # passing disturbance of the shared host link lands in one round of
+    # each rather than in one measurement; the medians are reported
+    e2e_rounds, copy_rounds = [], []
+    for _ in range(3):
+        e2e_rounds.append(e2e_time(KE))
+        last = h_out[(KE - 1) % NBUF][..., :W].numpy()
+        e2e_err = float(np.linalg.norm((last - ref).ravel()) / np.linalg.norm(ref.ravel()))
+        copy_rounds.append(e2e_time(KE, transform=False))
+    e2e_ms = max_over_ranks(statistics.median(e2e_rounds), dist)
+    copy_ms = max_over_ranks(statistics.median(copy_rounds), dist)
     e2e_bytes = h_in.numel() * 4
 
     extra = c2c1024_numbers(vd, torch, flush, args) if rank == 0 and not args.quick else {}
@@ -408,6 +414,7 @@ def _run_ours(args):
                 "h2d_bytes_per_step": e2e_bytes,
                 "d2h_bytes_per_step": e2e_bytes,
                 "pipelining": f"{NBUF} buffers, 3 streams",
+                "rounds": f"median of 3 rounds of {KE} steps, each round the loop then the copies alone",
                 "copies_alone_ms_per_step": round(copy_ms, 4),
                 "frac_of_copies_alone": round(copy_ms / e2e_ms, 3),
                 "error_rel_l2_vs_fp64": e2e_err,
