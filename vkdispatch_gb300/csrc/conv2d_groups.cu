@@ -157,14 +157,18 @@ int exec_groups(const vdx_group_plan* p, void* data, const void* kernel, void* s
   };
   if (p->groups == 1) return run(0, caller);
   cudaError_t e = cudaEventRecord(p->fork, caller);
+  int rc = VDX_OK;
   for (int g = 0; g < p->groups && e == cudaSuccess; ++g) {
     e = cudaStreamWaitEvent(p->side[g], p->fork, 0);
     if (e != cudaSuccess) break;
-    const int rc = run(g, p->side[g]);
-    if (rc != VDX_OK) return rc;
+    rc = run(g, p->side[g]);
+    // a group that has started is joined back even when one of its launches
+    // failed, so work the caller queues next never races with it
     e = cudaEventRecord(p->join[g], p->side[g]);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(caller, p->join[g], 0);
+    if (rc != VDX_OK) break;
   }
+  if (rc != VDX_OK) return rc;  // the failing launch's message stays in vdx_last_error
   if (e != cudaSuccess)
     return vdx::set_error(VDX_ERR_CUDA, (std::string("image groups: ") + cudaGetErrorString(e)).c_str());
   return VDX_OK;
