@@ -339,3 +339,92 @@ def test_codegen_abbreviations_module():
     assert ns["f32"] is vd.float32 and ns["v2"] is vd.vec2 and ns["c64"] is vd.complex64
     assert ns["Buff"][vd.float32].var_type is vd.float32
     assert callable(vd.make_context) and callable(vd.get_context)
+
+
+class _FakeImages:
+    """Stands in for a contiguous complex64 Buffer / RFFTBuffer of a batch
+    of images on the host: enough for the image-group dispatch, which only
+    reads shapes, sizes and the data pointer before recording a launch."""
+
+    def __init__(self, shape, real_shape=None, ptr=4096):
+        from vkdispatch_gb300 import dtypes as dt
+
+        self.shape = tuple(shape)
+        if real_shape is not None:
+            self.real_shape = tuple(real_shape)
+        self.size = 1
+        for d in shape:
+            self.size *= d
+        self.mem_size = 8 * self.size
+        self.var_type = dt.complex64
+        self.contiguous = True
+        self.ptr = ptr
+
+
+def _capture_chains(monkeypatch):
+    from vkdispatch_gb300.fft import functions as F
+
+    seen = []
+
+    class FakePlan:
+        def exec(self, *a):
+            raise AssertionError("a deferred CommandGraph must not launch")
+
+        def describe(self):
+            return {}
+
+    def fake(steps, groups):
+        seen.append((tuple(steps), groups))
+        return FakePlan()
+
+    monkeypatch.setattr(F.P, "get_group_plan", fake)
+    monkeypatch.setenv("VDX_CONV2D_STREAMS", "2")
+    return F, seen
+
+
+def test_image_group_chains_of_the_2d_functions(monkeypatch):
+    """Each batched 2-D function hands the group plan the reference's own
+    composition (vkdispatch/fft/functions.py:164-300, 373-448, 549-646):
+    transform kinds, axes, direction, normalisation and kernel broadcast."""
+    import vkdispatch_gb300 as vd
+    from vkdispatch_gb300 import _lib as L
+
+    F, seen = _capture_chains(monkeypatch)
+    C2C, R2C, C2R, CONV = L.VDX_KIND_C2C, L.VDX_KIND_R2C, L.VDX_KIND_C2R, L.VDX_KIND_CONV
+    img = _FakeImages((16, 512, 512))
+    rimg = _FakeImages((16, 512, 257), real_shape=(16, 512, 512))
+    g = vd.CommandGraph()
+
+    F.fft2(img, graph=g)
+    F.ifft2(img, graph=g, normalize=False)
+    F.rfft2(rimg, graph=g)
+    F.irfft2(rimg, graph=g)
+    F.convolve2D(img, _FakeImages((16, 512, 512), ptr=8192), graph=g)
+    F.convolve2DR(rimg, _FakeImages((1, 512, 257), ptr=8192), graph=g)  # one kernel for every image
+    F.convolve2DR(rimg, _FakeImages((16, 512, 257), ptr=8192), graph=g, normalize=False)
+    assert len(g) == 7
+    full, half, real = (16, 512, 512), (16, 512, 257), (16, 512, 512)
+    want = [
+        ((full, 1, C2C, False, False, False), (full, 2, C2C, False, False, False)),
+        ((full, 1, C2C, True, False, False), (full, 2, C2C, True, False, False)),
+        ((real, 2, R2C, False, False, False), (half, 1, C2C, False, False, False)),
+        ((half, 1, C2C, True, True, False), (real, 2, C2R, True, True, False)),
+        ((full, 2, C2C, False, False, False), (full, 1, CONV, False, True, False), (full, 2, C2C, True, True, False)),
+        ((real, 2, R2C, False, False, False), (half, 1, CONV, False, True, True), (real, 2, C2R, True, True, False)),
+        ((real, 2, R2C, False, False, False), (half, 1, CONV, False, False, False), (real, 2, C2R, True, False, False)),
+    ]
+    got = [tuple((tuple(s[0]), s[1], s[2], bool(s[3]), bool(s[4]), bool(s[5])) for s in steps) for steps, _ in seen]
+    assert got == want
+    assert all(groups == 2 for _, groups in seen)
+
+
+def test_image_groups_keep_a_small_kernel_refused(monkeypatch):
+    """A kernel buffer smaller than one image is refused with ValueError, as
+    the ungrouped convolution refuses it."""
+    import vkdispatch_gb300 as vd
+
+    F, seen = _capture_chains(monkeypatch)
+    rimg = _FakeImages((16, 512, 257), real_shape=(16, 512, 512))
+    with pytest.raises(ValueError):
+        F.convolve2DR(rimg, _FakeImages((1, 256, 257), ptr=8192), graph=vd.CommandGraph())
+    assert not seen
