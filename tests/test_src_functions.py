@@ -83,3 +83,24 @@ def test_plan_sources():
     before = vd.fft.get_cache_info()
     vd.fft.fft_src((256, 1024))
     assert vd.fft.get_cache_info().hits == before.hits + 1
+
+
+def test_shader_factories_are_cached_callables():
+    """vd.fft.make_fft_shader / make_convolution_shader / make_transpose_shader
+    (vkdispatch/fft/shader_factories.py:11-195): cached per argument tuple,
+    cleared by vd.fft.cache_clear, argument errors raised at creation."""
+    import pytest
+
+    import vkdispatch_gb300 as vd
+
+    a = vd.fft.make_fft_shader((8, 1024), 1, inverse=True)
+    assert a is vd.fft.make_fft_shader((8, 1024), 1, inverse=True)
+    assert a is not vd.fft.make_fft_shader((8, 1024), 1)
+    assert isinstance(a, vd.fft.ShaderFunction) and callable(a)
+    c = vd.fft.make_convolution_shader((8, 1024), kernel_num=2)
+    t = vd.fft.make_transpose_shader((8, 1024), axis=1)
+    assert "convolution" in c.name and "transpose" in t.name
+    with pytest.raises(ValueError):
+        vd.fft.make_convolution_shader((8, 1024), kernel_num=0)
+    vd.fft.cache_clear()
+    assert vd.fft.make_fft_shader((8, 1024), 1, inverse=True) is not a

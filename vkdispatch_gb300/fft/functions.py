@@ -964,4 +964,7 @@ def transpose(in_buffer: Buffer, conv_shape: Tuple = None, axis: int = None, out
 
 
 def cache_clear() -> None:
+    from . import shader_factories
+
     P.cache_clear()
+    shader_factories.cache_clear()
