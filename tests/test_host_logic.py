@@ -428,3 +428,26 @@ def test_image_groups_keep_a_small_kernel_refused(monkeypatch):
     with pytest.raises(ValueError):
         F.convolve2DR(rimg, _FakeImages((1, 256, 257), ptr=8192), graph=vd.CommandGraph())
     assert not seen
+
+
+def test_runtime_helpers_without_gpu(caplog):
+    """Top-level runtime helpers of the reference (vkdispatch/base/init.py:
+    366-380, 622-760): backend queries, logging through the Python logger
+    with the caller's location, and the log-level filter."""
+    import logging
+
+    import vkdispatch_gb300 as vd
+
+    assert vd.is_cuda() and not vd.is_vulkan() and not vd.is_dummy() and not vd.is_opencl()
+    vd.initialize()
+    assert vd.is_initialized()
+    with caplog.at_level(logging.DEBUG, logger="vkdispatch_gb300"):
+        vd.set_log_level(vd.LogLevel.WARNING)
+        vd.log_info("not shown")
+        vd.log_warning("shown")
+        vd.log_error("also shown")
+    msgs = [r.getMessage() for r in caplog.records if r.name == "vkdispatch_gb300"]
+    assert any("shown" in m and "test_host_logic.py" in m for m in msgs)
+    assert not any("not shown" in m for m in msgs)
+    vd.set_log_level(vd.LogLevel.INFO)
+    assert vd.get_cuda_capture() is None

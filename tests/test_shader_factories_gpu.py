@@ -61,3 +61,22 @@ def test_convolution_and_transpose_shaders():
     vd.fft.make_transpose_shader((16, 512), axis=1)(out, kb)
     torch.cuda.synchronize()
     assert np.array_equal(out.read(0)[: 16 * 512].reshape(16, 512), kb.read(0))
+
+
+def test_runtime_helpers_on_gpu():
+    """get_devices, the typed buffer allocators and the capture state that
+    cuda_graph_capture yields (vkdispatch/execution_pipeline/
+    cuda_graph_capture.py:9-41)."""
+    devs = vd.get_devices()
+    assert devs and devs[0].dev_index == 0 and devs[0].sub_group_size == 32
+    assert devs[0].device_name in repr(devs[0])
+    b = vd.buffer_c64((4, 8))
+    assert b.shape == (4, 8) and b.var_type == vd.complex64
+    assert vd.buffer_f32((3,)).var_type == vd.float32
+    s = torch.cuda.Stream()
+    with vd.cuda_graph_capture(s) as cap:
+        assert vd.get_cuda_capture() is cap and cap.cuda_stream is s
+        with vd.suspend_cuda_capture():
+            assert vd.get_cuda_capture() is None
+        assert vd.get_cuda_capture() is cap
+    assert vd.get_cuda_capture() is None

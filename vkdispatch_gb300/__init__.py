@@ -10,8 +10,6 @@ Kernels live in libvdx.so (include/vdx.h), called through ctypes; PyTorch
 provides device memory and streams.  There is no CPU fallback.
 """
 
-import enum as _enum
-
 from . import codegen  # noqa: F401
 from . import fft  # noqa: F401
 from . import reduce  # noqa: F401
@@ -34,14 +32,40 @@ from .dtypes import (  # noqa: F401
 )
 from .graph import (  # noqa: F401
     CommandGraph,
+    CUDAGraphCapture,
     cuda_graph_capture,
     default_graph,
+    get_cuda_capture,
     global_graph,
     queue_wait_idle,
     set_global_graph,
     suspend_cuda_capture,
 )
+from .fft.shader_factories import ShaderFunction  # noqa: F401
+from .fft.src_functions import ShaderSource  # noqa: F401
 from .reduce import MappingFunction, map  # noqa: F401
+from .runtime import (  # noqa: F401
+    DeviceInfo,
+    LogLevel,
+    buffer_c64,
+    buffer_f32,
+    buffer_f64,
+    buffer_i32,
+    buffer_u32,
+    buffer_v2,
+    get_devices,
+    is_context_initialized,
+    is_dummy,
+    is_initialized,
+    is_opencl,
+    log,
+    log_error,
+    log_info,
+    log_verbose,
+    log_warning,
+    set_log_level,
+)
+from . import runtime as _runtime  # noqa: E402
 
 __version__ = "0.1.0"
 
@@ -87,6 +111,7 @@ def make_context(devices=None, use_cpu: bool = False, **kwargs) -> Context:
         dev = int(devices[0] if isinstance(devices, (list, tuple)) else devices)
         torch.cuda.set_device(dev)
     _load_lib()
+    _runtime._mark_initialized()
     _context = Context(torch.cuda.current_device())
     return _context
 
@@ -98,6 +123,7 @@ def get_context() -> Context:
 def initialize(*args, **kwargs) -> None:
     """Loads libvdx (there is a single CUDA backend; arguments are ignored)."""
     _load_lib()
+    _runtime._mark_initialized()
 
 
 def is_cuda() -> bool:
@@ -112,11 +138,5 @@ def is_vulkan() -> bool:
     return False
 
 
-class LogLevel(_enum.IntEnum):
-    """Log levels vd.initialize(log_level=...) accepts (the reference's
-    vd.LogLevel); libvdx reports errors through exceptions and logs nothing."""
-
-    VERBOSE = 0
-    INFO = 1
-    WARNING = 2
-    ERROR = 3
+def _context_made() -> bool:
+    return _context is not None

@@ -102,23 +102,44 @@ def resolve(graph: Optional[CommandGraph]) -> CommandGraph:
 @contextlib.contextmanager
 def cuda_graph_capture(stream=None):
     """Routes every launch in the block to ``stream`` (default: torch's
-    current stream), e.g. inside ``torch.cuda.graph(g)``."""
-    prev = getattr(_tls, "stream", None)
+    current stream), e.g. inside ``torch.cuda.graph(g)``; yields the
+    capture state (vkdispatch/execution_pipeline/cuda_graph_capture.py:9-41)."""
+    prev, prev_cap = getattr(_tls, "stream", None), getattr(_tls, "capture", None)
     _tls.stream = _as_handle(stream) if stream is not None else int(torch.cuda.current_stream().cuda_stream)
+    cap = CUDAGraphCapture(stream if stream is not None else torch.cuda.current_stream())
+    _tls.capture = cap
     try:
-        yield
+        yield cap
     finally:
-        _tls.stream = prev
+        _tls.stream, _tls.capture = prev, prev_cap
 
 
 @contextlib.contextmanager
 def suspend_cuda_capture():
-    prev = getattr(_tls, "stream", None)
-    _tls.stream = None
+    prev, prev_cap = getattr(_tls, "stream", None), getattr(_tls, "capture", None)
+    _tls.stream = _tls.capture = None
     try:
         yield
     finally:
-        _tls.stream = prev
+        _tls.stream, _tls.capture = prev, prev_cap
+
+
+class CUDAGraphCapture:
+    """The state of one cuda_graph_capture block: the stream launches go to,
+    and the buffers the capture keeps alive (none are needed here: libvdx
+    launches take their arguments by value)."""
+
+    def __init__(self, cuda_stream):
+        self.cuda_stream = cuda_stream
+        self.uniform_buffers: List = []
+
+    def add_uniform_buffer(self, buffer) -> None:
+        self.uniform_buffers.append(buffer)
+
+
+def get_cuda_capture():
+    """The calling thread's active CUDAGraphCapture, or None."""
+    return getattr(_tls, "capture", None)
 
 
 def queue_wait_idle() -> None:
