@@ -5,8 +5,10 @@
  * stream, status codes and vdx_last_error().
  *
  *   vdx_c_consumer validate   argument checks only; needs no GPU
- *   vdx_c_consumer run        transforms on the GPU, checked against
- *                             double-precision DFTs computed here
+ *   vdx_c_consumer run        transforms on the GPU (C2C, convolve2DR image
+ *                             groups, a reduction, a batch of uneven
+ *                             lengths), checked against double-precision
+ *                             DFTs computed here
  *
  * Exit status 0 when every check passes.
  */
@@ -263,6 +265,56 @@ static void conv2d_check(double* err_groups, int* chain_equal) {
   free(got);
 }
 
+/* uneven lengths in one persistent launch: (length, count) items packed back
+ * to back in one buffer */
+static double check_batch(int* status) {
+  const int lens[4] = {12, 100, 1024, 4096}, counts[4] = {5, 3, 2, 1};
+  vdx_batch_item items[4];
+  long total = 0;
+  for (int i = 0; i < 4; ++i) {
+    items[i].offset = total;
+    items[i].length = lens[i];
+    items[i].count = counts[i];
+    total += (long)lens[i] * counts[i];
+  }
+  float* h = malloc(sizeof(float) * 2 * total);
+  cd* in = malloc(sizeof(cd) * total);
+  cd* ref = malloc(sizeof(cd) * total);
+  double* got = malloc(sizeof(double) * 2 * total);
+  for (long i = 0; i < total; ++i) {
+    h[2 * i] = (float)sin(0.013 * i + 0.3);
+    h[2 * i + 1] = (float)cos(0.007 * (double)(i * i % 977));
+    in[i].re = h[2 * i];
+    in[i].im = h[2 * i + 1];
+  }
+  for (int i = 0; i < 4; ++i)
+    for (int c = 0; c < counts[i]; ++c) {
+      const long o = items[i].offset + (long)c * lens[i];
+      dft(in + o, 1, ref + o, 1, lens[i], -1);
+    }
+  vdx_batch_plan* bp = NULL;
+  size_t ws_bytes = 0;
+  void *dev = NULL, *ws = NULL;
+  expect(vdx_batch_plan_create(items, 4, 0, 0, &bp) == VDX_OK, "batch plan");
+  expect(vdx_batch_workspace_bytes(bp, &ws_bytes) == VDX_OK, "batch workspace size");
+  expect(cudaMalloc(&dev, sizeof(float) * 2 * total) == cudaSuccess, "cudaMalloc");
+  if (ws_bytes) expect(cudaMalloc(&ws, ws_bytes) == cudaSuccess, "cudaMalloc workspace");
+  cudaMemcpy(dev, h, sizeof(float) * 2 * total, cudaMemcpyHostToDevice);
+  expect(vdx_batch_exec(bp, dev, ws, NULL) == VDX_OK, "batch exec");
+  expect(vdx_batch_status(bp, status) == VDX_OK, "batch status");
+  cudaMemcpy(h, dev, sizeof(float) * 2 * total, cudaMemcpyDeviceToHost);
+  for (long i = 0; i < 2 * total; ++i) got[i] = h[i];
+  const double err = rel_l2(got, (const double*)ref, 2 * total);
+  vdx_batch_plan_destroy(bp);
+  cudaFree(dev);
+  if (ws) cudaFree(ws);
+  free(h);
+  free(in);
+  free(ref);
+  free(got);
+  return err;
+}
+
 /* sum over rows of (3, 100000) float32 */
 static double check_reduce(void) {
   const int B = 3;
@@ -309,11 +361,14 @@ int main(int argc, char** argv) {
   int same = 0;
   conv2d_check(&e_conv, &same);
   const double e_red = check_reduce();
+  int bstatus = -1;
+  const double e_batch = check_batch(&bstatus);
   expect(e_fft < 1e-5, "C2C against the double DFT");
   expect(e_conv < 1e-5, "conv2d groups against the double reference");
   expect(same, "group chain equals the conv2d groups plan bit for bit");
   expect(e_red < 1e-5, "reduce against the double sum");
-  printf("run: %s c2c_rel_l2=%.3g conv2d_rel_l2=%.3g chain_bit_equal=%d reduce_rel=%.3g\n",
-         failures ? "FAILED" : "ok", e_fft, e_conv, same, e_red);
+  expect(e_batch < 1e-5 && bstatus == 0, "batched uneven lengths against the double DFT");
+  printf("run: %s c2c_rel_l2=%.3g conv2d_rel_l2=%.3g chain_bit_equal=%d reduce_rel=%.3g batch_rel_l2=%.3g\n",
+         failures ? "FAILED" : "ok", e_fft, e_conv, same, e_red, e_batch);
   return failures ? 1 : 0;
 }

@@ -2,8 +2,9 @@
 header compiles as C, the program links against the in-tree libvdx.so with
 no Python or torch in the process, and its checks pass -- argument
 validation on the CPU, and on the GPU a runtime-radix C2C, the convolve2DR
-image groups and a reduction against double-precision DFTs computed in C,
-with the three-step vdx_group_plan bit-equal to vdx_conv2d_groups."""
+image groups, a reduction and a persistent batch of uneven lengths against
+double-precision DFTs computed in C, with the three-step vdx_group_plan
+bit-equal to vdx_conv2d_groups."""
 
 import subprocess
 from pathlib import Path
