@@ -123,13 +123,17 @@ typedef struct vdx_fft_desc {
 
 typedef struct vdx_plan vdx_plan;
 
-/* Library version (major*10000 + minor*100 + patch). */
+/* Library version (major*10000 + minor*100 + patch).  No counterpart in the
+ * reference's path (its version is the Python package's). */
 int vdx_version(void);
 
-/* Copies the calling thread's last error message into buf (NUL-terminated). */
+/* Copies the calling thread's last error message into buf (NUL-terminated):
+ * the reference's polled error string (vkdispatch/base/errors.py:15-28). */
 int vdx_last_error(char* buf, size_t n);
 
-/* Number of visible CUDA devices; fails when the driver is unusable. */
+/* Number of visible CUDA devices; fails when the driver is unusable (the
+ * device count behind the reference's get_devices, vkdispatch/backends/
+ * cuda_backend/api_context.py:42-50). */
 int vdx_device_count(int* count);
 
 /*
@@ -151,7 +155,9 @@ int vdx_autotune_entries(int64_t* entries, int64_t* searches);
 int vdx_autotune_save(const char* path);
 int vdx_autotune_load(const char* path);
 
-/* Human-readable plan (radices, threads per transform, transforms per CTA). */
+/* Human-readable plan (radices, threads per transform, transforms per CTA):
+ * what print_shader / ShaderFunction.get_src show in the reference
+ * (vkdispatch/shader/shader_function.py:255-275), as JSON. */
 int vdx_fft_plan_describe(const vdx_plan* plan, char* buf, size_t n);
 
 /*
@@ -259,7 +265,8 @@ int vdx_group_plan_destroy(vdx_group_plan* plan);
 int vdx_group_plan_describe(const vdx_group_plan* plan, char* buf, size_t n);
 int vdx_group_exec(const vdx_group_plan* plan, void* data, const void* kernel, void* stream);
 
-/* Number of CTAs one vdx_fft_exec of this plan launches. */
+/* Number of CTAs one vdx_fft_exec of this plan launches (sizes the loss
+ * partials of vdx_fft_exec_ops).  No counterpart in the reference. */
 int vdx_fft_plan_ctas(const vdx_plan* plan, int64_t* ctas);
 
 /*
@@ -340,7 +347,8 @@ int vdx_batch_plan_set_wait(vdx_batch_plan* plan, int64_t wait_limit, int32_t ex
 /*
  * Number of stage-1 partial slots vdx_reduce needs per batch row for a row
  * of `n` elements; the workspace must hold partial_count * batch elements of
- * the output type.
+ * the output type.  The reference sizes the same stage from its workgroup
+ * count (vkdispatch/reduce/reduce_function.py:117-125).
  */
 int vdx_reduce_partial_count(int64_t n, int64_t* partial_count);
 
@@ -427,10 +435,15 @@ typedef struct vdx_map_args {
 } vdx_map_args;
 
 typedef struct vdx_map_plan vdx_map_plan;
+/* Plan creation compiles the mapped FFT shader (vkdispatch/fft/
+ * shader_factories.py:11-60 with maps; io_manager.py:107-155); exec is its
+ * launch (vkdispatch/shader/shader_function.py:277-380). */
 int vdx_map_plan_create(const vdx_fft_desc* desc, const char* hooks_source, vdx_map_plan** plan);
 int vdx_map_plan_destroy(vdx_map_plan* plan);
 int vdx_map_exec(const vdx_map_plan* plan, const vdx_map_args* args, void* stream);
-/* The full source NVRTC compiled for the plan (hooks and instantiation). */
+/* The full source NVRTC compiled for the plan (hooks and instantiation): the
+ * reference's ShaderFunction.get_src (vkdispatch/shader/shader_function.py:
+ * 258-275). */
 int vdx_map_plan_source(const vdx_map_plan* plan, char* buf, size_t n);
 
 /*
@@ -460,7 +473,8 @@ int vdx_reduce_map_exec(const vdx_reduce_map_plan* plan, const vdx_map_args* arg
 int vdx_reduce_map_plan_status(const vdx_reduce_map_plan* plan, int* status, int reset);
 int vdx_reduce_map_plan_source(const vdx_reduce_map_plan* plan, char* buf, size_t n);
 /* 1 when a launch of the plan indexed a map buffer out of range, else 0
- * (synchronous read; reset != 0 clears it). */
+ * (synchronous read; reset != 0 clears it).  No counterpart in the
+ * reference. */
 int vdx_map_plan_status(const vdx_map_plan* plan, int* status, int reset);
 
 #ifdef __cplusplus

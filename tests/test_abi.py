@@ -198,3 +198,20 @@ def test_group_plan_validation_without_gpu(specs, groups):
     assert L.lib().vdx_group_exec(None, None, None, None) == L.VDX_ERR_INVALID
     assert L.lib().vdx_group_plan_describe(None, None, 0) == L.VDX_ERR_INVALID
     assert L.lib().vdx_group_plan_destroy(None) == L.VDX_OK
+
+
+def test_every_entry_point_cites_the_reference():
+    """Each declaration of include/vdx.h sits under a comment that names the
+    reference interface it replaces (a vkdispatch/ file) or says it has no
+    counterpart there."""
+    src = HEADER.read_text()
+    last = ""
+    missing = []
+    for part in re.split(r"(/\*.*?\*/)", src, flags=re.S):
+        if part.startswith("/*"):
+            last = part
+            continue
+        for m in re.finditer(r"^int\s+(vdx_\w+)\s*\(", part, flags=re.M):
+            if "vkdispatch/" not in last and "counterpart" not in last.lower():
+                missing.append(m.group(1))
+    assert not missing, missing
