@@ -106,3 +106,38 @@ def test_get_src_of_fixed_and_compiled_maps(capsys):
     assert "VdxReduceHooks" in c1.code and "reduce_mapped_final" in c2.code
     max_map.print_src()
     assert "Reduction Stage 2" in capsys.readouterr().out
+
+
+def test_map_with_registers_and_control_flow():
+    """A mapping function that declares registers, assigns them in place and
+    branches before returning (the statements the reference's codegen emits
+    for such a map, vkdispatch/codegen/functions/control_flow.py) lowers to
+    the same statements ahead of the hook's return."""
+
+    def clipped(buf: vc.Buffer[vc.f32], lim: vc.Var[vc.f32]) -> vc.f32:
+        i = vd.reduce.mapped_io_index()
+        r = vc.new_float_register(buf[i])
+        with vc.if_block(r > lim):
+            r[:] = lim
+        with vc.else_if_block(r < -lim):
+            r[:] = -lim
+        with vc.else_block():
+            r += 1.0
+        c = vc.new_int_register(0)
+        with vc.while_block(c < 3):
+            c += 1
+            r *= 0.5
+        return r
+
+    src, slots = _reduce_hooks(vd.reduce.MappingFunction(clipped), (FakeBuffer((64,), vd.float32), 2.0))
+    assert "if (" in src and "else if (" in src and "while (" in src and slots.fscalars == [2.0]
+    assert src.index("while (") < src.index("return")
+    _compile(src, acc="float", op=0)
+
+
+def test_map_without_a_return_value_is_refused():
+    def nothing(buf: vc.Buffer[vc.f32]) -> vc.f32:
+        vc.new_float_register(buf[vd.reduce.mapped_io_index()])
+
+    with pytest.raises(NotImplementedError):
+        _reduce_hooks(vd.reduce.MappingFunction(nothing), (FakeBuffer((64,), vd.float32),))

@@ -129,3 +129,32 @@ def test_reference_preamble_and_abbreviations():
         return buffer[vd.reduce.mapped_io_index()]
 
     assert np.allclose([data.sum()], [sum_map(buf).read(0)[0]])
+
+
+def test_map_with_registers_and_control_flow():
+    """A mapping function with registers, in-place updates, an if / else-if /
+    else chain and a bounded while loop before its return value."""
+    rng = np.random.default_rng(7)
+    a = (rng.standard_normal(200003) * 3).astype(np.float32)
+    ba = vd.asbuffer(a)
+
+    @vd.reduce.map_reduce(vd.reduce.SubgroupAdd)
+    def clipped(buf: vc.Buffer[vc.f32], lim: vc.Var[vc.f32]) -> vc.f32:
+        i = vd.reduce.mapped_io_index()
+        r = vc.new_float_register(buf[i])
+        with vc.if_block(r > lim):
+            r[:] = lim
+        with vc.else_if_block(r < -lim):
+            r[:] = -lim
+        with vc.else_block():
+            r += 1.0
+        c = vc.new_int_register(0)
+        with vc.while_block(c < 3):
+            c += 1
+            r *= 0.5
+        return r
+
+    got = clipped(ba, 2.0).read(0)[0]
+    x = a.astype(np.float64)
+    ref = (np.where(x > 2.0, 2.0, np.where(x < -2.0, -2.0, x + 1.0)) * 0.125).sum()
+    assert abs(got - ref) <= 1e-5 * np.abs(x).sum()

@@ -217,17 +217,27 @@ def _reduce_hooks(mf: "MappingFunction", args):
     if len(args) != len(types):
         raise ValueError(f"map {mf.func.__name__} takes {len(types)} arguments, {len(args)} given")
     syms = [M._TraceScalar(i, t) if sc else vc.SymBuffer(i, t) for i, (t, sc) in enumerate(zip(types, flags))]
+    # registers, their assignments and control-flow blocks the map runs
+    # before its return value are recorded as events and lowered to the
+    # statements that precede the hook's return
+    events: list = []
+    M._tls.events, M._tls.nreg = events, 0
     try:
         r = mf.func(*syms)
     except NotImplementedError:
         raise
     except Exception as e:  # noqa: BLE001
         raise NotImplementedError(f"map {mf.func.__name__} could not be traced: {e}") from e
+    finally:
+        M._tls.events = None
+    if r is None:
+        raise NotImplementedError(f"map {mf.func.__name__} returns no value to reduce")
     slots = J.Slots()
     low = J._Lower(mf.func.__name__, types, flags, list(args), slots)
+    stmts = low.statements(events)
     code, _ = low.expr(r)
     body = ["using namespace vdx::mapops;", "const long long k = 0, n = 0;", "(void)k; (void)n; (void)m;",
-            f"return {code};"]
+            *stmts, f"return {code};"]
     src = "struct VdxReduceHooks {\n" + J._hook("auto map(const vdx::MapArgs& m, long long io)", body) + "};\n"
     return src, slots
 
