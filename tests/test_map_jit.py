@@ -261,3 +261,38 @@ def test_every_traced_math_function_lowers_and_compiles():
         assert f"m_{fn}(" in spec.source, fn
     _nvrtc_compile(spec.source, strided="false")
     _nvrtc_compile(spec.source, strided="true", re="double")  # the fp64-compute instantiation
+
+
+def test_control_flow_in_output_and_kernel_maps_compiles():
+    """Blocks in the store and spectrum hooks too: an output map that writes
+    one of two buffers by a condition, and a kernel map whose loop and
+    complex register updates run between the forward and inverse passes."""
+    out_a, out_b = FakeBuffer((6, 10), vd.complex64), FakeBuffer((6, 10), vd.complex64)
+    sig, ker = FakeBuffer((6, 10), vd.complex64), FakeBuffer((6, 10), vd.complex64)
+    mask = FakeBuffer((6, 10), vd.int32)
+
+    @vd.map
+    def split_store(a: vc.Buffer[vc.c64], b: vc.Buffer[vc.c64], keep: vc.Buffer[vc.i32]):
+        op = vd.fft.write_op()
+        with vc.if_block(vc.all(keep[op.io_index] != 0, op.fft_index < op.fft_size - 1)):
+            op.write_to_buffer(a)
+        with vc.else_block():
+            b[op.io_index] = op.register.conjugate()
+
+    @vd.map
+    def shaped_kernel(h: vc.Buffer[vc.c64], taps: vc.Var[vc.i32]):
+        op = vd.fft.read_op()
+        acc = vc.new_complex_register(0.0, 0.0)
+        t = vc.new_int_register(0)
+        with vc.while_block(t < taps):
+            acc += h[(op.io_index + t) % 60] * 0.5
+            t += 1
+        with vc.if_block(vc.abs(acc.real) > 1.0):
+            acc.real = vc.sign(acc.real)
+        op.register[:] = vc.mult_complex(op.register, acc.conjugate())
+
+    spec = J.build_hooks([out_a, out_b, mask], [sig], [ker, 3], None, split_store, shaped_kernel, True)
+    src = spec.source
+    assert src.count("{") == src.count("}") and "while (" in src and "else {" in src
+    _nvrtc_compile(src, strided="false", mode=2)  # the fused convolution runs the kernel hook
+    _nvrtc_compile(src, strided="true", mode=2, re="double")
