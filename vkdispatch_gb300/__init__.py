@@ -65,7 +65,7 @@ from .runtime import (  # noqa: F401
     log_warning,
     set_log_level,
 )
-from . import runtime as _runtime  # noqa: E402
+from . import runtime as _runtime
 
 __version__ = "0.1.0"
 
