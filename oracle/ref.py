@@ -34,6 +34,16 @@ def lib():
     return _lib
 
 
+def set_threads(n: int) -> int:
+    """Sets the OpenMP threads of the restatement's batched loops (a launcher
+    such as torchrun may have set OMP_NUM_THREADS=1 for the process) and
+    returns the count now in effect."""
+    L = lib()
+    L.omp_set_num_threads(ctypes.c_int(int(n)))
+    L.omp_get_max_threads.restype = ctypes.c_int
+    return int(L.omp_get_max_threads())
+
+
 def plan(n: int):
     """The reference planner's stage prime groups for length n, or None when
     the reference rejects n."""
