@@ -215,3 +215,24 @@ def test_every_entry_point_cites_the_reference():
             if "vkdispatch/" not in last and "counterpart" not in last.lower():
                 missing.append(m.group(1))
     assert not missing, missing
+
+
+@pytest.mark.parametrize("lang", ["c99", "c++11"])
+def test_header_compiles_as_strict_c_and_cpp(tmp_path, lang):
+    """A cgo, JNI or C++ host includes include/vdx.h as is: it compiles as
+    C99 and as C++11 with every warning an error."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc" if lang == "c99" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / "t.c"
+    src.write_text('#include "vdx.h"\nint main(void) { vdx_fft_desc d; vdx_batch_item b; (void)d; (void)b; '
+                   'return 0; }\n')
+    cmd = [cc, f"-std={lang}", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", str(HEADER.parent), "-c", str(src),
+           "-o", str(tmp_path / "t.o")]
+    if lang != "c99":
+        cmd[1:1] = ["-x", "c++"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
